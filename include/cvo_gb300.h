@@ -1,0 +1,274 @@
+/*
+ * cvo_gb300.h -- C ABI of the GB300-native CVO / RKHS-BA registration core.
+ *
+ * Drop-in boundary for the `cvo::CvoGPU` registration path of UMich-CURLY/RKHS_BA.
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (CVO_OK == 0) and never calls exit().  Each declaration cites the reference
+ * member it replaces (paths relative to the reference project root).
+ *
+ * Conventions kept from the reference:
+ *  - 4x4 matrices are COLUMN-MAJOR float[16] (Eigen default storage).
+ *  - cvo_align(): the target cloud is moved by inverse(T_init); the returned
+ *    T_out satisfies x_src ~= T_out * y_tgt   (src/cvo/CvoGPU.cu:98-116,1265-1467).
+ *  - cvo_function_angle()/cvo_inner_product(): the target is moved by inverse(T)
+ *    (src/cvo/CvoGPU.cpp:215-221, src/cvo/CvoGPU.cu:1685-1702).
+ *  - multi-frame poses are double[12], ROW-major 3x4 [R|t], frame -> world
+ *    (include/UnifiedCvo/cvo/CvoFrame.hpp:26).
+ *  - association rows are source indices, columns are target indices.
+ *
+ * Threading: one handle owns one CUDA stream and private device workspaces.
+ * Calls on one handle are blocking and must not be made concurrently.
+ */
+#ifndef CVO_GB300_H
+#define CVO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+  CVO_OK = 0,
+  CVO_ZERO_GRADIENT = -1,      /* align stopped on a zero gradient (CvoGPU.cu:1356-1360) */
+  CVO_ERR_INVALID_ARG = -2,
+  CVO_ERR_EMPTY_CLOUD = -3,    /* reference returns 0 / -1 / cos 0 on empty input (CvoGPU.cu:1492-1495,1526-1529,1573-1577) */
+  CVO_ERR_BAD_YAML = -4,
+  CVO_ERR_CUDA = -5,
+  CVO_ERR_OUT_OF_MEMORY = -6,
+  CVO_ERR_TIMEOUT = -7,
+  CVO_ERR_UNSUPPORTED = -8,
+  CVO_ERR_IO = -9,
+  CVO_ERR_CAPACITY = -10
+};
+
+/* -------------------------------------------------------------- parameters
+ * Field-for-field mirror of cvo::CvoParams (include/UnifiedCvo/cvo/CvoParams.hpp:12-79).
+ * cvo_params_default() reproduces the constructor defaults (:80-136); the
+ * reference leaves max_step uninitialised, here it defaults to 0.8 (the value of
+ * cvo_params/cvo_geometric_params_gpu.yaml).
+ */
+typedef struct cvo_params {
+  float ell_init_first_frame;
+  float ell_init;
+  float ell_min;
+  int   min_ell_iter_limit;
+  float ell_max;
+  double dl;
+  double dl_step;
+  float sigma;
+  float sp_thres;
+  float c;
+  float d;
+  float c_ell;
+  float c_sigma;
+  float s_ell;
+  float s_sigma;
+  int   MAX_ITER;
+  float eps;
+  float eps_2;
+  float min_step;
+  float max_step;
+  float step;
+  int   nearest_neighbors_max;
+  float ell_decay_rate;
+  float ell_decay_rate_first_frame;
+  int   ell_decay_start;
+  int   ell_decay_start_first_frame;
+  int   indicator_window_size;
+  float indicator_stable_threshold;
+  int   is_pcl_visualization_on;
+  int   is_using_least_square;
+  int   is_ell_adaptive;
+  int   is_full_ip_matrix;
+  int   is_using_geometry;
+  int   is_using_intensity;
+  int   is_using_semantics;
+  int   is_using_range_ell;
+  int   is_using_kdtree;
+  int   is_exporting_association;
+  int   is_using_geometric_type;
+  int   is_global_angle_registration;
+  int   multiframe_using_cpu;
+  int   multiframe_max_iters;
+  float multiframe_ell_init;
+  float multiframe_ell_min;
+  float multiframe_ell_max;
+  int   multiframe_iter_per_ell;
+  float multiframe_ell_decay_rate;
+  int   multiframe_iterations_per_ell;
+  int   multiframe_iterations_per_solve;
+  int   multiframe_expected_points;
+  float multiframe_downsample_voxel_size;
+  int   multiframe_num_neighbors;
+  int   multiframe_least_squares_num_threads;
+  int   multiframe_min_nonzeros;
+  int   multiframe_is_optimizing_ell;
+  int   multiframe_is_sorting_inner_product;
+  int   multiframe_is_free_memory_each_iter;
+} cvo_params;
+
+/* ------------------------------------------------------------------ clouds
+ * Host-side cloud descriptor; the caller owns the memory (as with the
+ * reference's CvoPointCloud, "ownership: user", src/cvo/CvoState.cuh:23-24).
+ * Replaces the AoS CvoPoint record (include/UnifiedCvo/utils/PointSegmentedDistribution.hpp:51-144).
+ *   xyz       : n * xyz_stride floats (stride 3 or 4; extra component ignored)
+ *   features  : n * F floats, row-major, values in [0,1] (NULL when F == 0)
+ *   labels    : n * C floats, row-major label distributions (NULL when C == 0)
+ *   geom_type : n * 2 floats (NULL unless is_using_geometric_type)
+ */
+typedef struct cvo_cloud {
+  int n;
+  int F;
+  int C;
+  int xyz_stride;
+  const float *xyz;
+  const float *features;
+  const float *labels;
+  const float *geom_type;
+} cvo_cloud;
+
+typedef struct cvo_handle cvo_handle;         /* replaces cvo::CvoGPU */
+typedef struct cvo_gpu_cloud cvo_gpu_cloud;   /* replaces CvoPointCloudGPU (thrust::device_vector<CvoPoint>) */
+typedef struct cvo_assoc cvo_assoc;           /* replaces cvo::Association (include/UnifiedCvo/cvo/Association.hpp:5-12) */
+
+/* ------------------------------------------------------------ parameters */
+/* CvoParams::CvoParams() defaults (CvoParams.hpp:80-136). */
+void cvo_params_default(cvo_params *p);
+/* read_CvoParams_yaml (CvoParams.hpp:203-323): sets only the keys present in the file. */
+int cvo_params_read_yaml(const char *yaml_path, cvo_params *inout);
+
+/* ---------------------------------------------------------------- handle */
+/* CvoGPU::CvoGPU(const std::string&) (src/cvo/CvoGPU.cu:65-74). */
+int cvo_create(const char *yaml_path, cvo_handle **out);
+/* Same as cvo_create with an explicit parameter block (no file). */
+int cvo_create_with_params(const cvo_params *p, cvo_handle **out);
+/* CvoGPU::~CvoGPU (src/cvo/CvoGPU.cu:83-86). */
+int cvo_destroy(cvo_handle *h);
+/* CvoGPU::get_params (include/UnifiedCvo/cvo/CvoGPU.hpp:66). */
+int cvo_get_params(const cvo_handle *h, cvo_params *out);
+/* CvoGPU::write_params (src/cvo/CvoGPU.cu:76-80); here both the host and device copies change. */
+int cvo_write_params(cvo_handle *h, const cvo_params *p);
+
+/* ----------------------------------------------------------- device clouds */
+/* CvoPointCloud_to_gpu (src/cvo/CvoGPU_impl.cu:220-289): upload once, reuse across calls. */
+int cvo_cloud_upload(cvo_handle *h, const cvo_cloud *c, cvo_gpu_cloud **out);
+int cvo_cloud_free(cvo_handle *h, cvo_gpu_cloud *c);
+int cvo_cloud_size(const cvo_gpu_cloud *c);
+
+/* ------------------------------------------------------------- two-view */
+/* int CvoGPU::align(src, tgt, T_init, T_out&, Association*, double* secs, int* iters)
+ * (src/cvo/CvoGPU.cu:1516-1563).  assoc may be NULL; it is filled only when
+ * params.is_exporting_association is set, as in the reference (:1468-1472).
+ * Returns CVO_OK or CVO_ZERO_GRADIENT (the reference's ret -1). */
+int cvo_align(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+              const float T_init[16], float T_out[16], cvo_assoc *assoc,
+              double *secs, int *iters);
+/* Device-resident variant of cvo_align (clouds already uploaded). */
+int cvo_align_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
+                  const float T_init[16], float T_out[16], cvo_assoc *assoc,
+                  double *secs, int *iters);
+/* CvoResultInfo CvoGPU::align(src, tgt, T_s2t, is_returning_association)
+ * (src/cvo/CvoGPU.cu:1566-1611): takes the source->target transform and
+ * inverts it before iterating.  ret_code receives the reference's return_code. */
+int cvo_align_s2t(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                  const float T_s2t[16], int want_assoc, float T_out[16],
+                  cvo_assoc *assoc, double *secs, int *iters, int *ret_code);
+
+/* Batched two-view align: n_pairs independent registrations in one persistent
+ * batch (one launch per kernel per iteration for all pairs).  srcs/tgts hold
+ * n_pairs device clouds (repeats allowed), T_init/T_out are n_pairs*16 floats.
+ * rets/iters are n_pairs ints (may be NULL).  No reference counterpart: it
+ * batches the loop of CvoGPU::align (src/cvo/CvoGPU.cu:1239-1477). */
+int cvo_align_batch_dev(cvo_handle *h, int n_pairs, cvo_gpu_cloud *const *srcs,
+                        cvo_gpu_cloud *const *tgts, const float *T_init,
+                        float *T_out, int *rets, int *iters, double *secs);
+
+/* ------------------------------------------------- inner product / angle */
+/* CvoGPU::inner_product_gpu (src/cvo/CvoGPU.cu:1734-1748): <f(X), f(T^-1 Y)> with
+ * the GPU semantics (range-scaled ell, first nearest_neighbors_max hits per row). */
+int cvo_inner_product(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                      const float T[16], float ell, float *out);
+int cvo_inner_product_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
+                          const float T[16], float ell, float *out);
+/* CvoGPU::inner_product_cpu (src/cvo/CvoGPU.cpp:204-231): host implementation
+ * with the reference CPU semantics (radius search, no neighbour cap, no range ell). */
+int cvo_inner_product_cpu(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                          const float T[16], float ell, float *out);
+/* CvoGPU::function_angle (src/cvo/CvoGPU.cu:1768-1806). */
+int cvo_function_angle(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                       const float T[16], float ell, int is_approximate, int is_gpu,
+                       float *out);
+/* Batched inner products of one source/target pair under n_poses transforms
+ * (n_poses*16 floats), all in one launch; out receives n_poses floats.  This is
+ * the batched form of the loop in CvoGPU::get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398). */
+int cvo_inner_product_batch_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
+                                int n_poses, const float *T, float ell, float *out);
+
+/* --------------------------------------------------------- association */
+/* CvoGPU::compute_association_gpu (src/cvo/CvoGPU.cu:1836-1871). */
+int cvo_compute_association(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                            const float T[16], float ell, cvo_assoc *out);
+int cvo_assoc_create(cvo_assoc **out);
+int cvo_assoc_destroy(cvo_assoc *a);
+/* Sizes of the stored association: rows (= source points), cols (= target points),
+ * nnz, and the number of source / target inlier entries. */
+int cvo_assoc_info(const cvo_assoc *a, int *rows, int *cols, int64_t *nnz,
+                   int64_t *n_source_inliers, int64_t *n_target_inliers);
+/* Copies the row-major CSR (row_ptr[rows+1], col[nnz], val[nnz], columns sorted
+ * ascending within each row) and the inlier lists.  Any pointer may be NULL. */
+int cvo_assoc_copy(const cvo_assoc *a, int64_t *row_ptr, int *col, float *val,
+                   int *source_inliers, int *target_inliers);
+
+/* --------------------------------------------------- global registration */
+/* CvoGPU::get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398): argmax of the
+ * approximate cos-angle over a rotation grid at ell.  grid_kind 0 selects the
+ * reference's 60-element icosahedral grid (gen_icosahedron_init_rots, :279-342);
+ * grid_kind 1 the 24-element octahedral grid; grid_kind 2 the n^3 roll-pitch-yaw
+ * grid of gen_rand_init_pose (:344-363) with n = num_guess.  T_out receives the
+ * chosen [rot|0] (source frame -> target frame), secs the elapsed seconds. */
+int cvo_get_nearest_init_pose(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                              float ell, int num_guess, int grid_kind,
+                              float T_out[16], double *secs);
+int cvo_get_nearest_init_pose_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
+                                  float ell, int num_guess, int grid_kind,
+                                  float T_out[16], double *secs);
+/* Rotation grids themselves (row-major 3x3 each): returns the count, writes up to
+ * max_rots rotations into rots (rots may be NULL to query the count). */
+int cvo_rotation_grid(int grid_kind, int num_guess, float *rots, int max_rots);
+
+/* Global registration of one pair from a set of initial poses: every hypothesis
+ * (n_hyp column-major 4x4 internal init poses, as taken by cvo_align) is refined
+ * by the batched align and judged by the final approximate cos-angle at
+ * judge_ell; the best pose is returned in T_out (cvo_align convention) and its
+ * index in best.  cos_out (n_hyp floats, may be NULL) receives every judged value. */
+int cvo_register_hypotheses_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
+                                int n_hyp, const float *T_init, float judge_ell,
+                                float T_out[16], int *best, float *cos_out, double *secs);
+
+/* ---------------------------------------------------------- multi-frame */
+/* CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670)
+ * -> CvoBatchIRLS::solve (src/cvo/IRLS.cpp:148-367).  poses: n_frames*12 doubles
+ * (row-major 3x4, frame->world), updated in place.  hold_const: n_frames bytes.
+ * edges: n_edges*2 frame indices.  iters receives the number of outer iterations. */
+int cvo_align_multi(cvo_handle *h, int n_frames, const cvo_cloud *clouds,
+                    double *poses, const uint8_t *hold_const, int n_edges,
+                    const int *edges, double *secs, int *iters);
+int cvo_align_multi_dev(cvo_handle *h, int n_frames, cvo_gpu_cloud *const *clouds,
+                        double *poses, const uint8_t *hold_const, int n_edges,
+                        const int *edges, double *secs, int *iters);
+
+/* -------------------------------------------------------------- misc */
+const char *cvo_status_string(int status);
+/* Number of kernel launches this handle has issued since creation (all kernels
+ * of this library; used by benchmarks to report launch counts). */
+int64_t cvo_kernel_launch_count(const cvo_handle *h);
+/* Last CUDA error text recorded by the handle (empty if none). */
+const char *cvo_last_error(const cvo_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CVO_GB300_H */

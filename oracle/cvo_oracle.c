@@ -1,0 +1,790 @@
+/*
+ * cvo_oracle.c -- CPU restatement of the reference CVO registration path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker used by tests/, by
+ * __graft_entry__.smoke() and by the cpu_baseline / reference arm of bench.py.
+ * The product library (rkhs_ba_gb300/csrc) never links, loads or calls it.
+ *
+ * Parity status: the reference (UMich-CURLY/RKHS_BA) cannot be compiled in this
+ * environment (Eigen, Sophus, PCL, TBB, Ceres, yaml-cpp absent) and its own
+ * tests hold no golden vectors for this path, so this oracle is "parity
+ * unpinned" against the reference binary: it is a line-by-line restatement of
+ * the reference's arithmetic (cited per function), pinned by property tests
+ * and by the committed fixtures under tests/golden/.
+ *
+ * Floating-point contract (shared with the CUDA kernels): every float
+ * operation that decides set membership (target transform, squared distances,
+ * range-scaled lengthscale, thresholds) is evaluated in a fixed order without
+ * fused multiply-add (build with -ffp-contract=off), so the GPU kernels, which
+ * use __fmul_rn/__fadd_rn in the same order, reproduce the same neighbour sets.
+ * Kernel values use double exp() exactly as the reference does
+ * (src/cvo/CvoGPU.cu:1023,1041,1050: the 2.0 literal promotes to double).
+ * Sums (gradient, step-size terms, inner products) are accumulated in double.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+#include <stdio.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "../include/cvo_gb300.h"
+
+#define ORC_TOLERANCE 1e-6f /* src/cvo/LieGroup.cpp:9 */
+#define ORC_PI 3.141592653589793
+#define ORC_TWO_PI_3 2.0943951023931957
+
+/* ------------------------------------------------------------ small helpers */
+
+static float cloud_x(const cvo_cloud *c, int i, int k) { return c->xyz[(size_t)i * c->xyz_stride + k]; }
+
+/* y' = Ri * y + Ti, canonical order ((r0*y0 + r1*y1) + r2*y2) + t.
+ * Follows transform_point_R_T (src/cvo/CvoGPU_impl.cu:32-83). */
+static void xform_pt(const float Ri[9], const float Ti[3], const float y[3], float out[3]) {
+  for (int r = 0; r < 3; r++) {
+    float a = Ri[3 * r + 0] * y[0];
+    float b = Ri[3 * r + 1] * y[1];
+    float c = Ri[3 * r + 2] * y[2];
+    out[r] = ((a + b) + c) + Ti[r];
+  }
+}
+
+/* From the internal pose (R,T) (column-major 4x4 float) to the target transform
+ * R_inv = R^T, T_inv = -R^T T (update_tf, src/cvo/CvoGPU.cu:98-130). */
+void orc_pose_to_rinv(const float T44[16], float Ri[9], float Ti[3]) {
+  float R[9], t[3];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) R[3 * r + c] = T44[c * 4 + r];
+    t[r] = T44[12 + r];
+  }
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) Ri[3 * r + c] = R[3 * c + r];
+  for (int r = 0; r < 3; r++) {
+    float a = Ri[3 * r + 0] * t[0];
+    float b = Ri[3 * r + 1] * t[1];
+    float c = Ri[3 * r + 2] * t[2];
+    Ti[r] = -((a + b) + c);
+  }
+}
+
+static float sqdist3(const float *a, const float *b) {
+  float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+  return (dx * dx + dy * dy) + dz * dz;   /* squared_dist, include/UnifiedCvo/cvo/gpu_utils.cuh:61-66 */
+}
+
+static float sqdist_n(const float *a, const float *b, int n) {
+  float r = 0.f;                          /* squared_dist<T>(a,b,dim), gpu_utils.cuh:33-40 */
+  for (int i = 0; i < n; i++) { float t = a[i] - b[i]; r += t * t; }
+  return r;
+}
+
+/* compute_range_ell (src/cvo/CvoGPU.cu:90-94); ||x|| in float as at :977. */
+static float range_norm(const float *x) { return sqrtf((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2]); }
+static float range_ell(float ell, float dist) { return (float)(((double)dist / 500.0 + 1.0) * (double)ell); }
+
+/* ---------------------------------------------------------- kernel constants */
+typedef struct {
+  float sigma2, c2, c_sigma2, s_ell, s_sigma2, sp_thres;
+  float log_geo;   /* logf(sp_thres / sigma2) */
+  float d2_c_thres, d2_s_thres;
+  int use_geo, use_int, use_sem, use_gtype;
+} kconst;
+
+static kconst make_kconst(const cvo_params *p) {
+  kconst k;
+  k.sigma2 = p->sigma * p->sigma;
+  k.c2 = p->c_ell * p->c_ell;
+  k.c_sigma2 = p->c_sigma * p->c_sigma;
+  k.s_ell = p->s_ell;
+  k.s_sigma2 = p->s_sigma * p->s_sigma;
+  k.sp_thres = p->sp_thres;
+  k.log_geo = logf(p->sp_thres / k.sigma2);
+  k.d2_c_thres = 1.f;
+  k.d2_s_thres = 1.f;
+  if (p->is_using_intensity) k.d2_c_thres = (float)(-2.0 * (double)k.c2 * (double)logf(p->sp_thres / k.c_sigma2));
+  if (p->is_using_semantics)
+    k.d2_s_thres = (float)(-2.0 * (double)k.s_ell * (double)k.s_ell * (double)logf(p->sp_thres / k.s_sigma2));
+  k.use_geo = p->is_using_geometry;
+  k.use_int = p->is_using_intensity;
+  k.use_sem = p->is_using_semantics;
+  k.use_gtype = p->is_using_geometric_type;
+  return k;
+}
+
+static float geo_d2_thres(const kconst *k, float l) { return (float)(-2.0 * (double)l * (double)l * (double)k->log_geo); }
+
+/* Pair kernel value of fill_in_A_mat_gpu (src/cvo/CvoGPU.cu:951-1099).
+ * Returns 1 and the value in *out if the pair is kept (a > sp_thres). */
+static int pair_value_gpu(const kconst *k, const cvo_params *p, const float *x, const float *fa,
+                          const float *la, const float *ga, const float *y, const float *fb,
+                          const float *lb, const float *gb, int F, int C, float l,
+                          float d2_thres, float *out) {
+  float ak = 1.f, sk = 1.f, ck = 1.f, kk = 1.f, geo_sim = 1.f;
+  if (k->use_gtype) {
+    float n2a = 0.f, n2b = 0.f, dab = 0.f;
+    for (int t = 0; t < 2; t++) { n2a += ga[t] * ga[t]; }
+    for (int t = 0; t < 2; t++) { n2b += gb[t] * gb[t]; }
+    for (int t = 0; t < 2; t++) { dab += ga[t] * gb[t]; }
+    geo_sim = dab * dab / (n2a * n2b);
+    if ((double)geo_sim < 0.01) return 0;
+  }
+  if (k->use_geo) {
+    float d2 = sqdist3(y, x);
+    if (d2 < d2_thres) kk = (float)((double)k->sigma2 * exp(-(double)d2 / (2.0 * (double)l * (double)l)));
+    else return 0;
+  }
+  if (k->use_int) {
+    float d2c = sqdist_n(fa, fb, F);
+    if (d2c < k->d2_c_thres) ck = (float)((double)k->c_sigma2 * exp(-(double)d2c / (2.0 * (double)k->c2)));
+    else return 0;
+  }
+  if (k->use_sem) {
+    float d2s = sqdist_n(la, lb, C);
+    if (d2s < k->d2_s_thres)
+      sk = (float)((double)(p->s_sigma * p->s_sigma) * exp(-(double)d2s / (2.0 * (double)k->s_ell * (double)k->s_ell)));
+    else return 0;
+  }
+  ak = ck * kk * sk * geo_sim;
+  if (ak > k->sp_thres) { *out = ak; return 1; }
+  return 0;
+}
+
+/* ------------------------------------------------------------ uniform grid */
+typedef struct { int64_t key; int j; } kj_t;
+typedef struct {
+  float h, ox, oy, oz;
+  int n;
+  kj_t *ent;      /* sorted by (key, j) */
+  int brute;      /* 1: no spatial pruning (all targets are candidates) */
+} grid_t;
+
+static int cmp_kj(const void *a, const void *b) {
+  const kj_t *x = (const kj_t *)a, *y = (const kj_t *)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return x->j - y->j;
+}
+static int cmp_int(const void *a, const void *b) { int x = *(const int *)a, y = *(const int *)b; return (x > y) - (x < y); }
+
+static int64_t cell_key(int64_t cx, int64_t cy, int64_t cz) {
+  return ((cx + (1 << 20)) << 42) | ((cy + (1 << 20)) << 21) | (cz + (1 << 20));
+}
+
+static void grid_build(grid_t *g, const float *pts, int n, float h) {
+  memset(g, 0, sizeof(*g));
+  g->n = n;
+  if (!(h > 0.f) || !isfinite(h)) { g->brute = 1; return; }
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int j = 0; j < n; j++)
+    for (int t = 0; t < 3; t++) { float v = pts[3 * j + t]; if (v < mn[t]) mn[t] = v; if (v > mx[t]) mx[t] = v; }
+  double ext = 0;
+  for (int t = 0; t < 3; t++) if (mx[t] - mn[t] > ext) ext = mx[t] - mn[t];
+  if (ext / h > 1.0e6) h = (float)(ext / 1.0e6);
+  g->h = h; g->ox = mn[0]; g->oy = mn[1]; g->oz = mn[2];
+  g->ent = (kj_t *)malloc(sizeof(kj_t) * (size_t)(n > 0 ? n : 1));
+  for (int j = 0; j < n; j++) {
+    int64_t cx = (int64_t)floor((pts[3 * j] - g->ox) / h);
+    int64_t cy = (int64_t)floor((pts[3 * j + 1] - g->oy) / h);
+    int64_t cz = (int64_t)floor((pts[3 * j + 2] - g->oz) / h);
+    g->ent[j].key = cell_key(cx, cy, cz);
+    g->ent[j].j = j;
+  }
+  qsort(g->ent, (size_t)n, sizeof(kj_t), cmp_kj);
+}
+static void grid_free(grid_t *g) { free(g->ent); g->ent = NULL; }
+
+/* Collect every target within the 27 neighbour cells of x, ascending index. */
+static int grid_candidates(const grid_t *g, const float *x, int *buf, int cap_buf) {
+  if (g->brute) { for (int j = 0; j < g->n && j < cap_buf; j++) buf[j] = j; return g->n; }
+  int64_t cx = (int64_t)floor((x[0] - g->ox) / g->h);
+  int64_t cy = (int64_t)floor((x[1] - g->oy) / g->h);
+  int64_t cz = (int64_t)floor((x[2] - g->oz) / g->h);
+  int cnt = 0;
+  for (int dx = -1; dx <= 1; dx++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dz = -1; dz <= 1; dz++) {
+        int64_t key = cell_key(cx + dx, cy + dy, cz + dz);
+        int lo = 0, hi = g->n;
+        while (lo < hi) { int mid = (lo + hi) / 2; if (g->ent[mid].key < key) lo = mid + 1; else hi = mid; }
+        for (int t = lo; t < g->n && g->ent[t].key == key; t++) { if (cnt < cap_buf) buf[cnt] = g->ent[t].j; cnt++; }
+      }
+  if (cnt <= cap_buf) qsort(buf, (size_t)cnt, sizeof(int), cmp_int);
+  return cnt;
+}
+
+/* ------------------------------------------------------------- A matrix */
+/* Sparse kernel matrix with the semantics of fill_in_A_mat_gpu
+ * (src/cvo/CvoGPU.cu:951-1099): range-scaled ell is always applied (:977-978),
+ * targets are scanned in ascending index and each row keeps the first `cap`
+ * kept pairs (:994-996).  ytr: transformed target xyz (m*3).  Outputs are ELL
+ * rows of width cap: ind (-1 padded), val, nnz per row. */
+int orc_fill_A(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float *ytr,
+               int cap, float ell, int *ind, float *val, int *nnz) {
+  int n = src->n, m = tgt->n, F = src->F, C = src->C;
+  kconst k = make_kconst(p);
+  /* grid cell >= largest geometric radius over the source rows */
+  float hmax = 0.f;
+  for (int i = 0; i < n; i++) {
+    float x[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
+    float l = range_ell(ell, range_norm(x));
+    float r = sqrtf(geo_d2_thres(&k, l));
+    if (r > hmax) hmax = r;
+  }
+  grid_t g;
+  grid_build(&g, ytr, m, k.use_geo ? hmax * 1.001f + 1e-6f : INFINITY);
+  int fail = 0;
+#pragma omp parallel
+  {
+    int bufcap = m > 0 ? m : 1;
+    int *buf = (int *)malloc(sizeof(int) * (size_t)bufcap);
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; i++) {
+      float x[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
+      float l = range_ell(ell, range_norm(x));
+      float d2t = 1.f;
+      if (k.use_geo) d2t = geo_d2_thres(&k, l);
+      int nc = grid_candidates(&g, x, buf, bufcap);
+      if (nc > bufcap) { fail = 1; nc = bufcap; }
+      int cnt = 0;
+      for (int t = 0; t < nc && cnt < cap; t++) {
+        int j = buf[t];
+        float a;
+        if (pair_value_gpu(&k, p, x, F ? src->features + (size_t)i * F : NULL, C ? src->labels + (size_t)i * C : NULL,
+                           src->geom_type ? src->geom_type + 2 * (size_t)i : NULL, ytr + 3 * (size_t)j,
+                           F ? tgt->features + (size_t)j * F : NULL, C ? tgt->labels + (size_t)j * C : NULL,
+                           tgt->geom_type ? tgt->geom_type + 2 * (size_t)j : NULL, F, C, l, d2t, &a)) {
+          ind[(size_t)i * cap + cnt] = j;
+          val[(size_t)i * cap + cnt] = a;
+          cnt++;
+        }
+      }
+      for (int t = cnt; t < cap; t++) { ind[(size_t)i * cap + t] = -1; val[(size_t)i * cap + t] = 0.f; }
+      nnz[i] = cnt;
+    }
+    free(buf);
+  }
+  grid_free(&g);
+  return fail ? -1 : 0;
+}
+
+/* Transform a whole cloud: out = Ri*y + Ti (m*3 floats). */
+void orc_transform(const float Ri[9], const float Ti[3], const cvo_cloud *c, float *out) {
+  for (int j = 0; j < c->n; j++) {
+    float y[3] = {cloud_x(c, j, 0), cloud_x(c, j, 1), cloud_x(c, j, 2)};
+    xform_pt(Ri, Ti, y, out + 3 * (size_t)j);
+  }
+}
+
+/* ------------------------------------------------------- gradient (flow) */
+/* compute_flow_gpu_no_eigen + compute_flow (src/cvo/CvoGPU.cu:2001-2120):
+ * omega = sum_ij a_ij (x_i x y_j) / c,  v = sum_ij a_ij (y_j - x_i) / d, in double. */
+void orc_flow(const cvo_params *p, const cvo_cloud *src, const float *ytr, int cap, const int *ind,
+              const float *val, const int *nnz, double out6[6]) {
+  int n = src->n;
+  double *rows = (double *)calloc((size_t)n * 6, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; i++) {
+    double x0 = cloud_x(src, i, 0), x1 = cloud_x(src, i, 1), x2 = cloud_x(src, i, 2);
+    double w[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+    for (int t = 0; t < nnz[i]; t++) {
+      int j = ind[(size_t)i * cap + t];
+      double a = val[(size_t)i * cap + t];
+      double y0 = ytr[3 * j], y1 = ytr[3 * j + 1], y2 = ytr[3 * j + 2];
+      w[0] += a * (x1 * y2 - x2 * y1);
+      w[1] += a * (x2 * y0 - x0 * y2);
+      w[2] += a * (x0 * y1 - x1 * y0);
+      v[0] += a * (y0 - x0);
+      v[1] += a * (y1 - x1);
+      v[2] += a * (y2 - x2);
+    }
+    for (int t = 0; t < 3; t++) { rows[6 * (size_t)i + t] = w[t] / (double)p->c; rows[6 * (size_t)i + 3 + t] = v[t] / (double)p->d; }
+  }
+  for (int t = 0; t < 6; t++) out6[t] = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int t = 0; t < 6; t++) out6[t] += rows[6 * (size_t)i + t];
+  free(rows);
+}
+
+/* Float normalisation of the stacked gradient (CvoGPU.cu:2096-2104). */
+void orc_normalize_grad(const double g[6], float xi[6]) {
+  float f[6];
+  for (int t = 0; t < 6; t++) f[t] = (float)g[t];
+  float s = 0.f;
+  for (int t = 0; t < 6; t++) s += f[t] * f[t];
+  if (s > 0.f) { float nr = sqrtf(s); for (int t = 0; t < 6; t++) f[t] = f[t] / nr; }
+  for (int t = 0; t < 6; t++) xi[t] = f[t];
+}
+
+/* ------------------------------------------------------------- step size */
+/* Taylor terms of compute_step_size_xi / compute_step_size_poly_coeff
+ * (src/cvo/CvoGPU.cu:333-462), evaluated in double. */
+void orc_step_terms(const cvo_params *p, const cvo_cloud *src, const float *ytr, int cap, const int *ind,
+                    const float *val, const int *nnz, const float xi[6], float ell, double out4[4]) {
+  int n = src->n;
+  double w[3] = {xi[0], xi[1], xi[2]}, vv[3] = {xi[3], xi[4], xi[5]};
+  double *rows = (double *)calloc((size_t)n * 4, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; i++) {
+    float xf[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
+    float tl = ell;
+    if (p->is_using_range_ell) tl = range_ell(ell, range_norm(xf));
+    double coef = 1.0 / (2.0 * (double)tl * (double)tl);
+    double B = 0, Cc = 0, D = 0, E = 0;
+    for (int t = 0; t < nnz[i]; t++) {
+      int j = ind[(size_t)i * cap + t];
+      double a = val[(size_t)i * cap + t];
+      double y[3] = {ytr[3 * j], ytr[3 * j + 1], ytr[3 * j + 2]};
+      double u[3], u2[3], u3[3], u4[3];
+      /* xi z = omega x y + v; xi^k z = omega x (xi^(k-1) z) for k >= 2 */
+      u[0] = w[1] * y[2] - w[2] * y[1] + vv[0];
+      u[1] = w[2] * y[0] - w[0] * y[2] + vv[1];
+      u[2] = w[0] * y[1] - w[1] * y[0] + vv[2];
+      u2[0] = w[1] * u[2] - w[2] * u[1]; u2[1] = w[2] * u[0] - w[0] * u[2]; u2[2] = w[0] * u[1] - w[1] * u[0];
+      u3[0] = w[1] * u2[2] - w[2] * u2[1]; u3[1] = w[2] * u2[0] - w[0] * u2[2]; u3[2] = w[0] * u2[1] - w[1] * u2[0];
+      u4[0] = w[1] * u3[2] - w[2] * u3[1]; u4[1] = w[2] * u3[0] - w[0] * u3[2]; u4[2] = w[0] * u3[1] - w[1] * u3[0];
+      double d[3] = {xf[0] - y[0], xf[1] - y[1], xf[2] - y[2]};
+      double normxiz2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+      double xiz_dot_xi2z = -(u[0] * u2[0] + u[1] * u2[1] + u[2] * u2[2]);
+      double epsil_const = (u2[0] * u2[0] + u2[1] * u2[1] + u2[2] * u2[2]) + 2.0 * (u[0] * u3[0] + u[1] * u3[1] + u[2] * u3[2]);
+      double ud = u[0] * d[0] + u[1] * d[1] + u[2] * d[2];
+      double u2d = u2[0] * d[0] + u2[1] * d[1] + u2[2] * d[2];
+      double u3d = u3[0] * d[0] + u3[1] * d[1] + u3[2] * d[2];
+      double u4d = u4[0] * d[0] + u4[1] * d[1] + u4[2] * d[2];
+      double beta = -2.0 * coef * ud;
+      double gamma = -coef * (normxiz2 + 2.0 * u2d);
+      double delta = 2.0 * coef * (xiz_dot_xi2z - u3d);
+      double epsil = -coef * (epsil_const + 2.0 * u4d);
+      B += a * beta;
+      Cc += a * (gamma + beta * beta / 2.0);
+      D += a * (delta + beta * gamma + beta * beta * beta / 6.0);
+      E += a * (epsil + beta * delta + 0.5 * beta * beta * gamma + 0.5 * gamma * gamma + beta * beta * beta * beta / 24.0);
+    }
+    rows[4 * (size_t)i] = B; rows[4 * (size_t)i + 1] = Cc; rows[4 * (size_t)i + 2] = D; rows[4 * (size_t)i + 3] = E;
+  }
+  for (int t = 0; t < 4; t++) out4[t] = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int t = 0; t < 4; t++) out4[t] += rows[4 * (size_t)i + t];
+  free(rows);
+}
+
+/* Roots of c3 s^3 + c2 s^2 + c1 s + c0 (closed form).  re/im receive 3 roots.
+ * Returns 0 if the cubic is degenerate (c3 == 0 or non-finite coefficients),
+ * which the reference's companion matrix turns into NaN eigenvalues
+ * (poly_solver_order3, src/cvo/LieGroup.cpp:310-326). */
+int orc_cubic_roots(double c3, double c2, double c1, double c0, double re[3], double im[3]) {
+  if (c3 == 0.0 || !isfinite(c3) || !isfinite(c2) || !isfinite(c1) || !isfinite(c0)) return 0;
+  double a = c2 / c3, b = c1 / c3, c = c0 / c3;
+  if (!isfinite(a) || !isfinite(b) || !isfinite(c)) return 0;
+  double a3 = a / 3.0;
+  double pp = b - a * a3;
+  double qq = 2.0 * a3 * a3 * a3 - a3 * b + c;
+  double disc = 0.25 * qq * qq + pp * pp * pp / 27.0;
+  if (disc > 0.0) {
+    double sd = sqrt(disc);
+    double uu = cbrt(-0.5 * qq + sd);
+    double vv = cbrt(-0.5 * qq - sd);
+    re[0] = uu + vv - a3; im[0] = 0.0;
+    re[1] = -0.5 * (uu + vv) - a3; im[1] = 0.5 * sqrt(3.0) * (uu - vv);
+    re[2] = re[1]; im[2] = -im[1];
+  } else if (pp == 0.0) {
+    double r = cbrt(-qq);
+    re[0] = re[1] = re[2] = r - a3; im[0] = im[1] = im[2] = 0.0;
+  } else {
+    double mm = 2.0 * sqrt(-pp / 3.0);
+    double arg = 3.0 * qq / (pp * mm);
+    if (arg > 1.0) arg = 1.0;
+    if (arg < -1.0) arg = -1.0;
+    double th = acos(arg) / 3.0;
+    for (int k = 0; k < 3; k++) { re[k] = mm * cos(th - ORC_TWO_PI_3 * k) - a3; im[k] = 0.0; }
+  }
+  return 1;
+}
+
+/* Step rule of compute_step_size (src/cvo/CvoGPU.cu:504-538): smallest positive
+ * real root of 4E s^3 + 3D s^2 + 2C s + B with |imag| < 1e-5, clamped. */
+double orc_step_from_terms(const cvo_params *p, const double bcde[4]) {
+  double re[3], im[3];
+  double temp = DBL_MAX;
+  if (orc_cubic_roots(4.0 * bcde[3], 3.0 * bcde[2], 2.0 * bcde[1], bcde[0], re, im)) {
+    for (int t = 0; t < 3; t++)
+      if (re[t] > 0 && re[t] < temp && fabs(im[t]) < 1e-5) temp = re[t];
+  }
+  if (temp > (double)p->max_step) return (double)p->max_step;
+  if (temp < (double)p->min_step) return (double)p->min_step;
+  return temp;
+}
+
+/* --------------------------------------------------------- Lie group */
+/* Exp_SEK3 for a 6-vector (src/cvo/LieGroup.cpp:245-275), float arithmetic.
+ * X: row-major 3x4. */
+void orc_exp_sek3(const float v[6], float dt, float X[12]) {
+  float w[3] = {v[0], v[1], v[2]};
+  float theta = sqrtf((w[0] * w[0] + w[1] * w[1]) + w[2] * w[2]);
+  float R[9], Jl[9];
+  if (theta < ORC_TOLERANCE) {
+    for (int t = 0; t < 9; t++) R[t] = Jl[t] = (t % 4 == 0) ? 1.f : 0.f;
+  } else {
+    float A[9] = {0.f, -w[2], w[1], w[2], 0.f, -w[0], -w[1], w[0], 0.f};
+    float A2[9];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) {
+        float s = A[3 * r] * A[c];
+        s = s + A[3 * r + 1] * A[3 + c];
+        s = s + A[3 * r + 2] * A[6 + c];
+        A2[3 * r + c] = s;
+      }
+    float theta2 = theta * theta;
+    float stheta = sinf(dt * theta);
+    float ctheta = cosf(dt * theta);
+    float omc = (1.f - ctheta) / theta2;
+    float s1 = stheta / theta;
+    float s3 = (dt * theta - stheta) / (theta2 * theta);
+    for (int t = 0; t < 9; t++) {
+      float I = (t % 4 == 0) ? 1.f : 0.f;
+      R[t] = (I + s1 * A[t]) + omc * A2[t];
+      Jl[t] = (dt * I + omc * A[t]) + s3 * A2[t];
+    }
+  }
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) X[4 * r + c] = R[3 * r + c];
+    float a = Jl[3 * r] * v[3], b = Jl[3 * r + 1] * v[4], c2 = Jl[3 * r + 2] * v[5];
+    X[4 * r + 3] = (a + b) + c2;
+  }
+}
+
+/* ||log(T)|| of an SE(3) element (Sophus::SE3d::log().norm(), used by
+ * dist_se3_cpu, src/cvo/CvoGPU.cpp:28-33), in double. */
+double orc_dist_se3(const double R[9], const double t[3]) {
+  double tr = R[0] + R[4] + R[8];
+  double cth = 0.5 * (tr - 1.0);
+  if (cth > 1.0) cth = 1.0;
+  if (cth < -1.0) cth = -1.0;
+  double th = acos(cth);
+  double vx = 0.5 * (R[7] - R[5]), vy = 0.5 * (R[2] - R[6]), vz = 0.5 * (R[3] - R[1]);
+  double w[3];
+  double sth = sin(th);
+  if (th < 1e-7) {
+    w[0] = vx; w[1] = vy; w[2] = vz;
+  } else if (ORC_PI - th < 1e-4) {
+    /* near pi: axis from the symmetric part */
+    double xx = sqrt(fmax(0.0, (R[0] + 1.0) * 0.5)), yy = sqrt(fmax(0.0, (R[4] + 1.0) * 0.5)), zz = sqrt(fmax(0.0, (R[8] + 1.0) * 0.5));
+    if (xx >= yy && xx >= zz) { yy = (R[1] + R[3]) / (4.0 * xx); zz = (R[2] + R[6]) / (4.0 * xx); }
+    else if (yy >= zz) { xx = (R[1] + R[3]) / (4.0 * yy); zz = (R[5] + R[7]) / (4.0 * yy); }
+    else { xx = (R[2] + R[6]) / (4.0 * zz); yy = (R[5] + R[7]) / (4.0 * zz); }
+    double nn = sqrt(xx * xx + yy * yy + zz * zz);
+    double sgn = (vx * xx + vy * yy + vz * zz) < 0 ? -1.0 : 1.0;
+    w[0] = sgn * th * xx / nn; w[1] = sgn * th * yy / nn; w[2] = sgn * th * zz / nn;
+  } else {
+    double f = th / sth;
+    w[0] = f * vx; w[1] = f * vy; w[2] = f * vz;
+  }
+  double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  double thn = sqrt(th2);
+  double W[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+  double W2[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) W2[3 * r + c] = W[3 * r] * W[c] + W[3 * r + 1] * W[3 + c] + W[3 * r + 2] * W[6 + c];
+  double k2;
+  if (thn < 1e-7) k2 = 1.0 / 12.0;
+  else {
+    double half = 0.5 * thn;
+    k2 = (1.0 - thn * cos(half) / (2.0 * sin(half))) / th2;
+  }
+  double u[3];
+  for (int r = 0; r < 3; r++) {
+    double s = t[r];
+    for (int c = 0; c < 3; c++) s += (-0.5 * W[3 * r + c] + k2 * W2[3 * r + c]) * t[c];
+    u[r] = s;
+  }
+  return sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2] + th2);
+}
+
+/* ------------------------------------------------------------ indicator */
+/* A_sparsity_indicator_ell_update (src/cvo/CvoGPU.cu:547-665). */
+typedef struct {
+  float qs[4096], qe[4096];
+  int qs_head, qs_len, qe_head, qe_len;
+  float ssum, esum;
+} indq_t;
+
+static void q_push(float *q, int *head, int *len, float v) { q[(*head + *len) % 4096] = v; (*len)++; }
+static float q_front(const float *q, int head) { return q[head % 4096]; }
+static void q_pop(int *head, int *len) { *head = (*head + 1) % 4096; (*len)--; }
+
+static int indicator_update(indq_t *s, float ind, const cvo_params *p) {
+  int decrease = 0;
+  int L = p->indicator_window_size;
+  if (s->qs_len < L) { q_push(s->qs, &s->qs_head, &s->qs_len, ind); s->ssum += ind; }
+  if (s->qs_len >= L && s->qe_len < L) { q_push(s->qe, &s->qe_head, &s->qe_len, ind); s->esum += ind; }
+  if (s->qs_len >= L && s->qe_len >= L) {
+    float ratio = s->esum / s->ssum;
+    if (ratio > 1.f - p->indicator_stable_threshold && ratio < 1.f + p->indicator_stable_threshold) {
+      decrease = 1;
+      s->qs_head = s->qs_len = s->qe_head = s->qe_len = 0;
+      s->ssum = 0.f; s->esum = 0.f;
+    } else {
+      float f = q_front(s->qe, s->qe_head);
+      s->esum -= f;
+      s->ssum += f;
+      q_push(s->qs, &s->qs_head, &s->qs_len, f);
+      q_pop(&s->qe_head, &s->qe_len);
+      s->ssum -= q_front(s->qs, s->qs_head);
+      q_pop(&s->qs_head, &s->qs_len);
+      q_push(s->qe, &s->qe_head, &s->qe_len, ind);
+      s->esum += ind;
+    }
+  }
+  return decrease;
+}
+
+/* --------------------------------------------------------------- align */
+/* Per-iteration trace (optional, may be NULL): ell, step, nnz, dist. */
+typedef struct {
+  float *ell; double *step; int64_t *nnz; double *dist; float *xi; int max_len;
+} orc_trace;
+
+/* align_impl (src/cvo/CvoGPU.cu:1239-1477).  T_init is the internal initial
+ * pose (column-major 4x4), T_out receives [R^T, -R^T T].  Returns 0 or -1. */
+int orc_align(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
+              float T_out[16], int *iters_out, orc_trace *trace) {
+  int n = src->n, m = tgt->n;
+  if (n == 0 || m == 0) { if (iters_out) *iters_out = 0; return 0; }
+  float R[9], T[3];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) R[3 * r + c] = T_init[c * 4 + r];
+    T[r] = T_init[12 + r];
+  }
+  int capmax = p->nearest_neighbors_max;
+  int cap = capmax;
+  float ell = p->ell_init;
+  int *ind = (int *)malloc(sizeof(int) * (size_t)n * (capmax > 0 ? capmax : 1));
+  float *val = (float *)malloc(sizeof(float) * (size_t)n * (capmax > 0 ? capmax : 1));
+  int *nnz = (int *)malloc(sizeof(int) * (size_t)n);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)m);
+  indq_t *q = (indq_t *)calloc(1, sizeof(indq_t));
+  int ret = 0, k = 0;
+  for (; k < p->MAX_ITER; k++) {
+    float T44[16] = {0};
+    for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T44[c * 4 + r] = R[3 * r + c]; T44[12 + r] = T[r]; }
+    T44[15] = 1.f;
+    float Ri[9], Ti[3];
+    orc_pose_to_rinv(T44, Ri, Ti);
+    orc_transform(Ri, Ti, tgt, ytr);
+    /* the ELL rows are laid out with the current cap as stride, like the reference */
+    orc_fill_A(p, src, tgt, ytr, cap, ell, ind, val, nnz);
+    int64_t nnz_sum = 0; int max_row = 0;
+    for (int i = 0; i < n; i++) { nnz_sum += nnz[i]; if (nnz[i] > max_row) max_row = nnz[i]; }
+    double g[6];
+    orc_flow(p, src, ytr, cap, ind, val, nnz, g);
+    float xi[6];
+    orc_normalize_grad(g, xi);
+    double bcde[4];
+    orc_step_terms(p, src, ytr, cap, ind, val, nnz, xi, ell, bcde);
+    double step = orc_step_from_terms(p, bcde);
+    float wn = sqrtf((xi[0] * xi[0] + xi[1] * xi[1]) + xi[2] * xi[2]);
+    float vn = sqrtf((xi[3] * xi[3] + xi[4] * xi[4]) + xi[5] * xi[5]);
+    if (trace && k < trace->max_len) {
+      if (trace->ell) trace->ell[k] = ell;
+      if (trace->step) trace->step[k] = step;
+      if (trace->nnz) trace->nnz[k] = nnz_sum;
+      if (trace->xi) for (int t = 0; t < 6; t++) trace->xi[6 * k + t] = xi[t];
+    }
+    if ((double)wn < (double)p->eps && (double)vn < (double)p->eps) {
+      if (wn < 1e-8f && vn < 1e-8f) ret = -1;
+      break;
+    }
+    float X[12];
+    orc_exp_sek3(xi, (float)step, X);
+    double dR[9], dT[3], Rd[9], Td[3];
+    for (int r = 0; r < 3; r++) {
+      for (int c = 0; c < 3; c++) dR[3 * r + c] = X[4 * r + c];
+      dT[r] = X[4 * r + 3];
+    }
+    for (int t = 0; t < 9; t++) Rd[t] = R[t];
+    for (int t = 0; t < 3; t++) Td[t] = T[t];
+    for (int r = 0; r < 3; r++) {
+      double s = Rd[3 * r] * dT[0];
+      s = s + Rd[3 * r + 1] * dT[1];
+      s = s + Rd[3 * r + 2] * dT[2];
+      T[r] = (float)(s + Td[r]);
+    }
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) {
+        double s = Rd[3 * r] * dR[c];
+        s = s + Rd[3 * r + 1] * dR[3 + c];
+        s = s + Rd[3 * r + 2] * dR[6 + c];
+        R[3 * r + c] = (float)s;
+      }
+    double dist = orc_dist_se3(dR, dT);
+    if (trace && k < trace->max_len && trace->dist) trace->dist[k] = dist;
+    float ip_curr = (float)((double)nnz_sum / sqrt((double)n * (double)m));
+    int need_decay = indicator_update(q, ip_curr, p);
+    if (dist < (double)p->eps_2) break;
+    if (k > p->ell_decay_start && need_decay) {
+      ell = ell * p->ell_decay_rate;
+      if (ell < p->ell_min) ell = p->ell_min;
+    }
+    int nc = (int)((double)max_row * 1.2);
+    cap = capmax < nc ? capmax : nc;
+  }
+  if (iters_out) *iters_out = k;
+  float T44[16] = {0};
+  for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T44[c * 4 + r] = R[3 * r + c]; T44[12 + r] = T[r]; }
+  T44[15] = 1.f;
+  float Ri[9], Ti[3];
+  orc_pose_to_rinv(T44, Ri, Ti);
+  memset(T_out, 0, sizeof(float) * 16);
+  for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T_out[c * 4 + r] = Ri[3 * r + c]; T_out[12 + r] = Ti[r]; }
+  T_out[15] = 1.f;
+  free(ind); free(val); free(nnz); free(ytr); free(q);
+  return ret;
+}
+
+/* --------------------------------------------------------- inner products */
+/* inner_product_impl (src/cvo/CvoGPU.cu:1673-1732): GPU semantics, cap =
+ * nearest_neighbors_max, sum of the sparse matrix.  Also returns nnz. */
+double orc_inner_product_gpu(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
+                             float ell, int64_t *nnz_out) {
+  int n = src->n, m = tgt->n;
+  if (n == 0 || m == 0) { if (nnz_out) *nnz_out = 0; return 0.0; }
+  int cap = p->nearest_neighbors_max;
+  float Ri[9], Ti[3];
+  orc_pose_to_rinv(T, Ri, Ti);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)m);
+  orc_transform(Ri, Ti, tgt, ytr);
+  int *ind = (int *)malloc(sizeof(int) * (size_t)n * (cap > 0 ? cap : 1));
+  float *val = (float *)malloc(sizeof(float) * (size_t)n * (cap > 0 ? cap : 1));
+  int *nnz = (int *)malloc(sizeof(int) * (size_t)n);
+  orc_fill_A(p, src, tgt, ytr, cap, ell, ind, val, nnz);
+  double s = 0.0; int64_t z = 0;
+  for (int i = 0; i < n; i++) {
+    double r = 0.0;
+    for (int t = 0; t < nnz[i]; t++) r += val[(size_t)i * cap + t];
+    s += r; z += nnz[i];
+  }
+  if (nnz_out) *nnz_out = z;
+  free(ytr); free(ind); free(val); free(nnz);
+  return s;
+}
+
+/* Fill the sparse matrix with GPU semantics at pose T and return it as ELL
+ * (helper for association tests). */
+int orc_association(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16], float ell,
+                    int cap, int *ind, float *val, int *nnz) {
+  float Ri[9], Ti[3];
+  orc_pose_to_rinv(T, Ri, Ti);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)(tgt->n > 0 ? tgt->n : 1));
+  orc_transform(Ri, Ti, tgt, ytr);
+  int r = orc_fill_A(p, src, tgt, ytr, cap, ell, ind, val, nnz);
+  free(ytr);
+  return r;
+}
+
+/* inner_product_cpu + se_kernel_init_ell_cpu (src/cvo/CvoGPU.cpp:113-231):
+ * radius search with squared radius -2 l^2 ln(sp/sigma^2) (strict <, as
+ * nanoflann's RadiusResultSet), no neighbour cap, no range ell, no colour or
+ * semantic thresholds, geometric-type term not applied. */
+double orc_inner_product_cpu(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
+                             float ell, int64_t *nnz_out) {
+  int n = src->n, m = tgt->n, F = src->F, C = src->C;
+  if (n == 0 || m == 0) { if (nnz_out) *nnz_out = 0; return 0.0; }
+  float Ri[9], Ti[3];
+  orc_pose_to_rinv(T, Ri, Ti);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)m);
+  orc_transform(Ri, Ti, tgt, ytr);
+  float s2 = p->sigma * p->sigma;
+  float l = ell;
+  float d2_thres = (float)(-2.0 * (double)l * (double)l * (double)logf(p->sp_thres / s2));
+  grid_t g;
+  grid_build(&g, ytr, m, sqrtf(d2_thres) * 1.001f + 1e-6f);
+  double total = 0.0; int64_t z = 0;
+  double *rows = (double *)calloc((size_t)n, sizeof(double));
+  int64_t *rz = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+#pragma omp parallel
+  {
+    int *buf = (int *)malloc(sizeof(int) * (size_t)m);
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; i++) {
+      float x[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
+      int nc = grid_candidates(&g, x, buf, m);
+      double r = 0.0; int64_t zz = 0;
+      for (int t = 0; t < nc; t++) {
+        int j = buf[t];
+        const float *y = ytr + 3 * (size_t)j;
+        float dx = x[0] - y[0], dy = x[1] - y[1], dz = x[2] - y[2];
+        float d2 = dx * dx; d2 += dy * dy; d2 += dz * dz;
+        if (!(d2 < d2_thres)) continue;
+        float kk = 1.f, ck = 1.f, sk = 1.f;
+        if (p->is_using_semantics) {
+          float d2s = sqdist_n(src->labels + (size_t)i * C, tgt->labels + (size_t)j * C, C);
+          sk = (float)((double)(p->s_sigma * p->s_sigma) * exp(-(double)d2s / (2.0 * (double)p->s_ell * (double)p->s_ell)));
+        }
+        if (p->is_using_geometry) kk = (float)((double)s2 * exp(-(double)d2 / (2.0 * (double)l * (double)l)));
+        if (p->is_using_intensity) {
+          float d2c = sqdist_n(src->features + (size_t)i * F, tgt->features + (size_t)j * F, F);
+          ck = (float)((double)(p->c_sigma * p->c_sigma) * exp(-(double)d2c / (2.0 * (double)p->c_ell * (double)p->c_ell)));
+        }
+        float a = ck * kk * sk;
+        if (a > p->sp_thres) { r += a; zz++; }
+      }
+      rows[i] = r; rz[i] = zz;
+    }
+    free(buf);
+  }
+  for (int i = 0; i < n; i++) { total += rows[i]; z += rz[i]; }
+  if (nnz_out) *nnz_out = z;
+  free(rows); free(rz); free(ytr); grid_free(&g);
+  return total;
+}
+
+/* function_angle (src/cvo/CvoGPU.cu:1768-1806). */
+double orc_function_angle(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
+                          float ell, int is_approximate, int is_gpu) {
+  if (src->n == 0 || tgt->n == 0) return 0.0;
+  float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  double fxfz = is_gpu ? orc_inner_product_gpu(p, src, tgt, T, ell, NULL) : orc_inner_product_cpu(p, src, tgt, T, ell, NULL);
+  double fx, fz;
+  if (is_approximate) { fx = (float)sqrt((double)src->n); fz = (float)sqrt((double)tgt->n); }
+  else if (is_gpu) { fx = sqrtf((float)orc_inner_product_gpu(p, src, src, I, ell, NULL)); fz = sqrtf((float)orc_inner_product_gpu(p, tgt, tgt, I, ell, NULL)); }
+  else { fx = sqrtf((float)orc_inner_product_cpu(p, src, src, I, ell, NULL)); fz = sqrtf((float)orc_inner_product_cpu(p, tgt, tgt, I, ell, NULL)); }
+  return (double)((float)fxfz / ((float)fx * (float)fz));
+}
+
+/* get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398) over a given rotation
+ * list (row-major 3x3 each).  Returns the chosen index, writes [rot|0]. */
+int orc_nearest_init_pose(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, float ell,
+                          const float *rots, int nrot, float T_out[16], float *cos_all) {
+  float best = 0.f; int bi = -1;
+  for (int r = 0; r < nrot; r++) {
+    float Tinv[16] = {0};
+    /* init_inv = [rot^T | 0] */
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) Tinv[b * 4 + a] = rots[9 * r + 3 * b + a];
+    Tinv[15] = 1.f;
+    float ip = (float)orc_function_angle(p, src, tgt, Tinv, ell, 1, 1);
+    if (cos_all) cos_all[r] = ip;
+    if (ip > best) { best = ip; bi = r; }
+  }
+  memset(T_out, 0, sizeof(float) * 16);
+  T_out[0] = T_out[5] = T_out[10] = T_out[15] = 1.f;
+  if (bi >= 0)
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) T_out[b * 4 + a] = rots[9 * bi + 3 * a + b];
+  return bi;
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}

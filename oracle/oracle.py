@@ -1,0 +1,244 @@
+"""ctypes wrapper of the C oracle (oracle/cvo_oracle.c), built by ``build()``.
+
+TEST INFRASTRUCTURE ONLY: the checker for tests/, __graft_entry__.smoke() and
+the CPU baseline of bench.py.  Parity is unpinned against the reference binary
+(it cannot be compiled here); the oracle restates the reference's arithmetic.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "cvo_oracle.c")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libcvo_oracle.so")
+CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=c11"]
+
+_L = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (no fused multiply-add) into oracle/_build/."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["gcc"] + CFLAGS + ["-I" + os.path.join(HERE, "..", "include"), SRC, "-o", LIB + ".tmp", "-lm"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def _lib():
+    global _L
+    if _L is None:
+        build()
+        _L = C.CDLL(LIB)
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int)
+        dp = C.POINTER(C.c_double)
+        vp = C.c_void_p
+        sig = {
+            "orc_fill_A": (C.c_int, [vp, vp, vp, fp, C.c_int, C.c_float, ip, fp, ip]),
+            "orc_transform": (None, [fp, fp, vp, fp]),
+            "orc_pose_to_rinv": (None, [fp, fp, fp]),
+            "orc_flow": (None, [vp, vp, fp, C.c_int, ip, fp, ip, dp]),
+            "orc_normalize_grad": (None, [dp, fp]),
+            "orc_step_terms": (None, [vp, vp, fp, C.c_int, ip, fp, ip, fp, C.c_float, dp]),
+            "orc_cubic_roots": (C.c_int, [C.c_double] * 4 + [dp, dp]),
+            "orc_step_from_terms": (C.c_double, [vp, dp]),
+            "orc_exp_sek3": (None, [fp, C.c_float, fp]),
+            "orc_dist_se3": (C.c_double, [dp, dp]),
+            "orc_align": (C.c_int, [vp, vp, vp, fp, fp, ip, vp]),
+            "orc_inner_product_gpu": (C.c_double, [vp, vp, vp, fp, C.c_float, C.POINTER(C.c_int64)]),
+            "orc_inner_product_cpu": (C.c_double, [vp, vp, vp, fp, C.c_float, C.POINTER(C.c_int64)]),
+            "orc_function_angle": (C.c_double, [vp, vp, vp, fp, C.c_float, C.c_int, C.c_int]),
+            "orc_association": (C.c_int, [vp, vp, vp, fp, C.c_float, C.c_int, ip, fp, ip]),
+            "orc_nearest_init_pose": (C.c_int, [vp, vp, vp, C.c_float, fp, C.c_int, fp, fp]),
+            "orc_num_threads": (C.c_int, []),
+            "orc_set_num_threads": (None, [C.c_int]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(_L, k)
+            f.restype = r
+            f.argtypes = a
+    return _L
+
+
+class OrcTrace(C.Structure):
+    _fields_ = [("ell", C.POINTER(C.c_float)), ("step", C.POINTER(C.c_double)),
+                ("nnz", C.POINTER(C.c_int64)), ("dist", C.POINTER(C.c_double)),
+                ("xi", C.POINTER(C.c_float)), ("max_len", C.c_int)]
+
+
+_fp = C.POINTER(C.c_float)
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _m16(T):
+    return _f(np.asarray(T, np.float32).reshape(4, 4).T.reshape(16))
+
+
+def _pp(params):
+    return C.cast(C.byref(params._c), C.c_void_p)
+
+
+def _pc(cs):
+    return C.cast(C.byref(cs), C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    _lib().orc_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(_lib().orc_num_threads())
+
+
+def transform_target(T, cloud) -> np.ndarray:
+    """Target positions moved by inverse(T) in the canonical float order."""
+    Ri = np.zeros(9, np.float32)
+    Ti = np.zeros(3, np.float32)
+    Tm = _m16(T)
+    L = _lib()
+    L.orc_pose_to_rinv(Tm.ctypes.data_as(_fp), Ri.ctypes.data_as(_fp), Ti.ctypes.data_as(_fp))
+    out = np.zeros((cloud.num_points(), 3), np.float32)
+    cs = cloud.c_struct()
+    L.orc_transform(Ri.ctypes.data_as(_fp), Ti.ctypes.data_as(_fp), _pc(cs), out.ctypes.data_as(_fp))
+    return out
+
+
+def association(params, src, tgt, T, ell, cap=None):
+    """ELL kernel matrix with GPU semantics: returns (ind (n, cap), val (n, cap), nnz (n,))."""
+    cap = params.nearest_neighbors_max if cap is None else cap
+    n = src.num_points()
+    ind = np.zeros((n, max(cap, 1)), np.int32)
+    val = np.zeros((n, max(cap, 1)), np.float32)
+    nnz = np.zeros(n, np.int32)
+    s, t = src.c_struct(), tgt.c_struct()
+    Tm = _m16(T)
+    _lib().orc_association(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), float(ell), int(cap),
+                           ind.ctypes.data_as(C.POINTER(C.c_int)), val.ctypes.data_as(_fp),
+                           nnz.ctypes.data_as(C.POINTER(C.c_int)))
+    return ind[:, :cap], val[:, :cap], nnz
+
+
+def flow(params, src, ytr, ind, val, nnz):
+    cap = ind.shape[1]
+    out = np.zeros(6, np.float64)
+    s = src.c_struct()
+    ind = np.ascontiguousarray(ind, np.int32)
+    val = np.ascontiguousarray(val, np.float32)
+    nnz = np.ascontiguousarray(nnz, np.int32)
+    ytr = _f(ytr)
+    _lib().orc_flow(_pp(params), _pc(s), ytr.ctypes.data_as(_fp), cap, ind.ctypes.data_as(C.POINTER(C.c_int)),
+                    val.ctypes.data_as(_fp), nnz.ctypes.data_as(C.POINTER(C.c_int)),
+                    out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def normalize_grad(g):
+    g = np.ascontiguousarray(g, np.float64)
+    xi = np.zeros(6, np.float32)
+    _lib().orc_normalize_grad(g.ctypes.data_as(C.POINTER(C.c_double)), xi.ctypes.data_as(_fp))
+    return xi
+
+
+def step_terms(params, src, ytr, ind, val, nnz, xi, ell):
+    cap = ind.shape[1]
+    out = np.zeros(4, np.float64)
+    s = src.c_struct()
+    ind = np.ascontiguousarray(ind, np.int32)
+    val = np.ascontiguousarray(val, np.float32)
+    nnz = np.ascontiguousarray(nnz, np.int32)
+    ytr = _f(ytr)
+    xi = _f(xi)
+    _lib().orc_step_terms(_pp(params), _pc(s), ytr.ctypes.data_as(_fp), cap, ind.ctypes.data_as(C.POINTER(C.c_int)),
+                          val.ctypes.data_as(_fp), nnz.ctypes.data_as(C.POINTER(C.c_int)), xi.ctypes.data_as(_fp),
+                          float(ell), out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def step_from_terms(params, bcde):
+    b = np.ascontiguousarray(bcde, np.float64)
+    return float(_lib().orc_step_from_terms(_pp(params), b.ctypes.data_as(C.POINTER(C.c_double))))
+
+
+def cubic_roots(c3, c2, c1, c0):
+    re = np.zeros(3)
+    im = np.zeros(3)
+    ok = _lib().orc_cubic_roots(c3, c2, c1, c0, re.ctypes.data_as(C.POINTER(C.c_double)),
+                                im.ctypes.data_as(C.POINTER(C.c_double)))
+    return bool(ok), re, im
+
+
+def exp_sek3(v, dt):
+    v = _f(v)
+    X = np.zeros(12, np.float32)
+    _lib().orc_exp_sek3(v.ctypes.data_as(_fp), float(dt), X.ctypes.data_as(_fp))
+    return X.reshape(3, 4)
+
+
+def dist_se3(R, t):
+    R = np.ascontiguousarray(R, np.float64).reshape(9)
+    t = np.ascontiguousarray(t, np.float64).reshape(3)
+    return float(_lib().orc_dist_se3(R.ctypes.data_as(C.POINTER(C.c_double)), t.ctypes.data_as(C.POINTER(C.c_double))))
+
+
+def align(params, src, tgt, T_init, trace_len: int = 0):
+    """align_impl restated on the CPU.  Returns (ret, T_out (4x4), iters, trace dict)."""
+    s, t = src.c_struct(), tgt.c_struct()
+    Ti = _m16(T_init)
+    To = np.zeros(16, np.float32)
+    iters = C.c_int(0)
+    tr = None
+    arrays = {}
+    if trace_len > 0:
+        arrays = dict(ell=np.zeros(trace_len, np.float32), step=np.zeros(trace_len), nnz=np.zeros(trace_len, np.int64),
+                      dist=np.zeros(trace_len), xi=np.zeros((trace_len, 6), np.float32))
+        tr = OrcTrace(arrays["ell"].ctypes.data_as(_fp), arrays["step"].ctypes.data_as(C.POINTER(C.c_double)),
+                      arrays["nnz"].ctypes.data_as(C.POINTER(C.c_int64)),
+                      arrays["dist"].ctypes.data_as(C.POINTER(C.c_double)), arrays["xi"].ctypes.data_as(_fp), trace_len)
+    ret = _lib().orc_align(_pp(params), _pc(s), _pc(t), Ti.ctypes.data_as(_fp), To.ctypes.data_as(_fp),
+                           C.byref(iters), C.cast(C.byref(tr), C.c_void_p) if tr is not None else None)
+    return ret, To.reshape(4, 4).T.copy(), iters.value, arrays
+
+
+def inner_product_gpu_semantics(params, src, tgt, T, ell):
+    s, t = src.c_struct(), tgt.c_struct()
+    Tm = _m16(T)
+    z = C.c_int64(0)
+    v = _lib().orc_inner_product_gpu(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), float(ell), C.byref(z))
+    return float(v), int(z.value)
+
+
+def inner_product_cpu_semantics(params, src, tgt, T, ell):
+    s, t = src.c_struct(), tgt.c_struct()
+    Tm = _m16(T)
+    z = C.c_int64(0)
+    v = _lib().orc_inner_product_cpu(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), float(ell), C.byref(z))
+    return float(v), int(z.value)
+
+
+def function_angle(params, src, tgt, T, ell, is_approximate=True, is_gpu=True):
+    s, t = src.c_struct(), tgt.c_struct()
+    Tm = _m16(T)
+    return float(_lib().orc_function_angle(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), float(ell),
+                                           int(is_approximate), int(is_gpu)))
+
+
+def nearest_init_pose(params, src, tgt, ell, rots):
+    rots = _f(np.asarray(rots).reshape(-1, 9))
+    nr = rots.shape[0]
+    s, t = src.c_struct(), tgt.c_struct()
+    To = np.zeros(16, np.float32)
+    cos = np.zeros(nr, np.float32)
+    bi = _lib().orc_nearest_init_pose(_pp(params), _pc(s), _pc(t), float(ell), rots.ctypes.data_as(_fp), nr,
+                                      To.ctypes.data_as(_fp), cos.ctypes.data_as(_fp))
+    return bi, To.reshape(4, 4).T.copy(), cos

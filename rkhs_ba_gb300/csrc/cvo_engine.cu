@@ -1,0 +1,785 @@
+// cvo_engine.cu -- batched, device-resident CVO iteration engine.
+//
+// The reference's align loop (align_impl, src/cvo/CvoGPU.cu:1239-1477) runs on
+// the host with about ten blocking host<->device crossings per iteration.  Here
+// the whole iteration, including its scalar tail (step size, pose update,
+// lengthscale schedule, neighbour-cap update, stopping tests), runs on the GPU
+// for every pair of a batch; the host only relaunches a captured CUDA graph of
+// `kChunk` iterations and reads one counter of unfinished pairs per chunk.
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+#include <chrono>
+#include "cvo_internal.h"
+#include "cvo_kernels.cuh"
+#include "cvo_lie.cuh"
+
+namespace cvo_gb {
+
+namespace {
+
+constexpr int kChunk = 8;
+
+// ------------------------------------------------------------------ reduce
+// Per-pair FP64 sums of the per-row partials written by k_assoc / k_overflow.
+__global__ void __launch_bounds__(kReduceThreads) k_reduce(BatchDev B, KParams K) {
+  __shared__ double sh[kReduceThreads / 32][10];
+  __shared__ bool last;
+  const int blk = blockIdx.x;
+  if (blk >= B.total_rblocks) return;
+  const int p = find_segment(B.rblk_off, B.npairs, blk);
+  PairDev *P = &B.pairs[p];
+  if (P->done) return;
+  const int b = blk - B.rblk_off[p];
+  const int nb = B.rblk_off[p + 1] - B.rblk_off[p];
+  const int n = P->n;
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int mx = 0;
+  for (int r = b * kReduceRows + threadIdx.x; r < min(n, (b + 1) * kReduceRows); r += kReduceThreads) {
+    const float4 *rs = reinterpret_cast<const float4 *>(P->row_sums + (size_t)r * 8);
+    float4 a0 = rs[0], a1 = rs[1];
+    acc[0] += a0.x; acc[1] += a0.y; acc[2] += a0.z; acc[3] += a0.w;
+    acc[4] += a1.x; acc[5] += a1.y; acc[6] += a1.z;
+    int z = P->nnz_row[r];
+    acc[7] += (double)z;
+    mx = max(mx, z);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 8; k++) acc[k] = warp_sum(acc[k]);
+  mx = warp_maxi(mx);
+  if (lane == 0) {
+    for (int k = 0; k < 8; k++) sh[w][k] = acc[k];
+    sh[w][8] = (double)mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int ww = 0; ww < kReduceThreads / 32; ww++) {
+      for (int k = 0; k < 8; k++) out[k] += sh[ww][k];
+      out[8] = fmax(out[8], sh[ww][8]);
+    }
+    for (int k = 0; k < 9; k++) P->part[(size_t)b * kPartStride + k] = out[k];
+    __threadfence();
+    unsigned prev = atomicAdd(&P->counter[0], 1u);
+    last = (prev == (unsigned)(nb - 1));
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  volatile double *pv = P->part;
+  for (int bb = 0; bb < nb; bb++) {
+    for (int k = 0; k < 8; k++) tot[k] += pv[(size_t)bb * kPartStride + k];
+    tot[8] = fmax(tot[8], pv[(size_t)bb * kPartStride + 8]);
+  }
+  P->counter[0] = 0;
+  for (int k = 0; k < 6; k++) P->grad[k] = tot[k];
+  P->asum = tot[6];
+  P->nnz_sum = (long long)tot[7];
+  P->max_row = (int)tot[8];
+  if (P->mode == MODE_ALIGN) {
+    // float normalisation of the stacked gradient (CvoGPU.cu:2096-2104)
+    float f[6];
+    for (int k = 0; k < 6; k++) f[k] = (float)tot[k];
+    float s = 0.f;
+    for (int k = 0; k < 6; k++) s = fa(s, fm(f[k], f[k]));
+    if (s > 0.f) {
+      float nr = __fsqrt_rn(s);
+      for (int k = 0; k < 6; k++) f[k] = __fdiv_rn(f[k], nr);
+    }
+    for (int k = 0; k < 6; k++) P->xi[k] = f[k];
+  }
+}
+
+// Picks the finest grid level whose cells serve the largest search radius.
+__device__ void choose_level(PairDev *P, const KParams &K, float max_norm) {
+  float l = range_ell(P->ell, max_norm);
+  float r = K.use_geo ? sqrtf(geo_d2_thres(l, K.log_geo)) : 0.f;
+  int lv = P->nlevels - 1;
+  for (int i = 0; i < P->nlevels; i++)
+    if (P->level_r[i] >= r) { lv = i; break; }
+  P->level = lv;
+  P->rq_max = r;
+}
+
+__device__ void pose_to_rinv(PairDev *P) {
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) P->Ri[3 * r + c] = P->R[3 * c + r];
+  for (int r = 0; r < 3; r++) {
+    float a = fm(P->Ri[3 * r], P->T[0]), b = fm(P->Ri[3 * r + 1], P->T[1]), c = fm(P->Ri[3 * r + 2], P->T[2]);
+    P->Ti[r] = -fa(fa(a, b), c);
+  }
+}
+
+// A_sparsity_indicator_ell_update (src/cvo/CvoGPU.cu:547-665) on ring buffers.
+__device__ bool indicator_update(PairDev *P, const KParams &K, float ind) {
+  const int L = K.indicator_window_size;
+  const int Q = kMaxIndicatorWindow;
+  bool decrease = false;
+  auto push = [&](float *q, int &head, int &len, float v) { q[(head + len) % Q] = v; len++; };
+  if (P->qs_len < L) { push(P->qs, P->qs_head, P->qs_len, ind); P->ssum = fa(P->ssum, ind); }
+  if (P->qs_len >= L && P->qe_len < L) { push(P->qe, P->qe_head, P->qe_len, ind); P->esum = fa(P->esum, ind); }
+  if (P->qs_len >= L && P->qe_len >= L) {
+    float ratio = __fdiv_rn(P->esum, P->ssum);
+    if (ratio > fs(1.f, K.indicator_stable_threshold) && ratio < fa(1.f, K.indicator_stable_threshold)) {
+      decrease = true;
+      P->qs_head = P->qs_len = P->qe_head = P->qe_len = 0;
+      P->ssum = 0.f; P->esum = 0.f;
+    } else {
+      float f = P->qe[P->qe_head % Q];
+      P->esum = fs(P->esum, f);
+      P->ssum = fa(P->ssum, f);
+      push(P->qs, P->qs_head, P->qs_len, f);
+      P->qe_head = (P->qe_head + 1) % Q; P->qe_len--;
+      P->ssum = fs(P->ssum, P->qs[P->qs_head % Q]);
+      P->qs_head = (P->qs_head + 1) % Q; P->qs_len--;
+      push(P->qe, P->qe_head, P->qe_len, ind);
+      P->esum = fa(P->esum, ind);
+    }
+  }
+  return decrease;
+}
+
+// Scalar tail of one iteration of align_impl (src/cvo/CvoGPU.cu:1339-1433).
+__device__ void finalize_iteration(BatchDev &B, PairDev *P, const KParams &K, float src_max_norm) {
+  const int k = P->iter;
+  double step = step_from_terms(P->bcde, (double)K.min_step, (double)K.max_step);
+  P->step = step;
+  const float *xi = P->xi;
+  float wn = __fsqrt_rn(fa(fa(fm(xi[0], xi[0]), fm(xi[1], xi[1])), fm(xi[2], xi[2])));
+  float vn = __fsqrt_rn(fa(fa(fm(xi[3], xi[3]), fm(xi[4], xi[4])), fm(xi[5], xi[5])));
+  P->level_used = P->level;
+  if ((double)wn < (double)K.eps && (double)vn < (double)K.eps) {
+    if (wn < 1e-8f && vn < 1e-8f) P->ret = -1;
+    P->done = 1;
+    atomicSub(B.active, 1);
+    return;
+  }
+  float X[12];
+  exp_sek3(xi, (float)step, X);
+  double dR[9], dT[3];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) dR[3 * r + c] = X[4 * r + c];
+    dT[r] = X[4 * r + 3];
+  }
+  double Rd[9], Td[3];
+  for (int t = 0; t < 9; t++) Rd[t] = P->R[t];
+  for (int t = 0; t < 3; t++) Td[t] = P->T[t];
+  for (int r = 0; r < 3; r++) {
+    double s = dm(Rd[3 * r], dT[0]);
+    s = da(s, dm(Rd[3 * r + 1], dT[1]));
+    s = da(s, dm(Rd[3 * r + 2], dT[2]));
+    P->T[r] = __double2float_rn(da(s, Td[r]));
+  }
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      double s = dm(Rd[3 * r], dR[c]);
+      s = da(s, dm(Rd[3 * r + 1], dR[3 + c]));
+      s = da(s, dm(Rd[3 * r + 2], dR[6 + c]));
+      P->R[3 * r + c] = __double2float_rn(s);
+    }
+  double dist = dist_se3(dR, dT);
+  P->dist = dist;
+  float ip_curr = __double2float_rn(__ddiv_rn((double)P->nnz_sum, sqrt(dm((double)P->n, (double)P->m))));
+  bool need_decay = indicator_update(P, K, ip_curr);
+  pose_to_rinv(P);
+  if (dist < (double)K.eps_2) {
+    P->done = 1;
+    atomicSub(B.active, 1);
+    return;
+  }
+  if (k > K.ell_decay_start && need_decay) {
+    P->ell = fm(P->ell, K.ell_decay_rate);
+    if (P->ell < K.ell_min) P->ell = K.ell_min;
+  }
+  int nc = (int)((double)P->max_row * 1.2);
+  P->cap = min(P->capmax, nc);
+  P->iter = k + 1;
+  if (P->iter >= K.max_iter) {
+    P->done = 1;
+    atomicSub(B.active, 1);
+    return;
+  }
+  choose_level(P, K, src_max_norm);
+}
+
+// -------------------------------------------------------------------- step
+// Taylor step-size terms (compute_step_size_xi + compute_step_size_poly_coeff,
+// src/cvo/CvoGPU.cu:333-462) per ELL row in FP32, FP64 across rows; the last
+// block of a pair finishes the iteration.
+__global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, const float *src_max_norm) {
+  __shared__ double sh[kStepThreads / 32][4];
+  __shared__ bool last;
+  const int blk = blockIdx.x;
+  if (blk >= B.total_sblocks) return;
+  const int p = find_segment(B.sblk_off, B.npairs, blk);
+  PairDev *P = &B.pairs[p];
+  if (P->done) return;
+  const int b = blk - B.sblk_off[p];
+  const int nb = B.sblk_off[p + 1] - B.sblk_off[p];
+  const int n = P->n;
+  const int s = b * kStepThreads + threadIdx.x;
+  float Bs = 0.f, Cs = 0.f, Ds = 0.f, Es = 0.f;
+  if (s < n) {
+    const float w0 = P->xi[0], w1 = P->xi[1], w2 = P->xi[2];
+    const float u0v = P->xi[3], u1v = P->xi[4], u2v = P->xi[5];
+    float4 x = __ldg(&P->xs[s]);
+    float tl = K.use_range_ell_step ? range_ell(P->ell, x.w) : P->ell;
+    float coef = __double2float_rn(__ddiv_rn(1.0, dm(dm(2.0, (double)tl), (double)tl)));
+    const int z = P->nnz_row[s];
+    const float4 *__restrict__ ycur = P->ycur;
+    for (int c = 0; c < z; c++) {
+      int t = P->A_j[(size_t)c * n + s];
+      float a = P->A_v[(size_t)c * n + s];
+      float4 y = __ldg(&ycur[t]);
+      float ux = w1 * y.z - w2 * y.y + u0v, uy = w2 * y.x - w0 * y.z + u1v, uz = w0 * y.y - w1 * y.x + u2v;
+      float px = w1 * uz - w2 * uy, py = w2 * ux - w0 * uz, pz = w0 * uy - w1 * ux;          // xi^2 z
+      float qx = w1 * pz - w2 * py, qy = w2 * px - w0 * pz, qz = w0 * py - w1 * px;          // xi^3 z
+      float rx = w1 * qz - w2 * qy, ry = w2 * qx - w0 * qz, rz = w0 * qy - w1 * qx;          // xi^4 z
+      float dx = x.x - y.x, dy = x.y - y.y, dz = x.z - y.z;
+      float normxiz2 = ux * ux + uy * uy + uz * uz;
+      float xiz_dot_xi2z = -(ux * px + uy * py + uz * pz);
+      float epsil_const = (px * px + py * py + pz * pz) + 2.f * (ux * qx + uy * qy + uz * qz);
+      float beta = -2.f * coef * (ux * dx + uy * dy + uz * dz);
+      float gamma = -coef * (normxiz2 + 2.f * (px * dx + py * dy + pz * dz));
+      float delta = 2.f * coef * (xiz_dot_xi2z - (qx * dx + qy * dy + qz * dz));
+      float epsil = -coef * (epsil_const + 2.f * (rx * dx + ry * dy + rz * dz));
+      float b2 = beta * beta;
+      Bs += a * beta;
+      Cs += a * (gamma + 0.5f * b2);
+      Ds += a * (delta + beta * gamma + b2 * beta * (1.f / 6.f));
+      Es += a * (epsil + beta * delta + 0.5f * b2 * gamma + 0.5f * gamma * gamma + b2 * b2 * (1.f / 24.f));
+    }
+  }
+  double v[4] = {Bs, Cs, Ds, Es};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 4; k++) v[k] = warp_sum(v[k]);
+  if (lane == 0)
+    for (int k = 0; k < 4; k++) sh[w][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double o[4] = {0, 0, 0, 0};
+    for (int ww = 0; ww < kStepThreads / 32; ww++)
+      for (int k = 0; k < 4; k++) o[k] += sh[ww][k];
+    for (int k = 0; k < 4; k++) P->part[(size_t)b * kPartStride + k] = o[k];
+    __threadfence();
+    unsigned prev = atomicAdd(&P->counter[1], 1u);
+    last = (prev == (unsigned)(nb - 1));
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double tot[4] = {0, 0, 0, 0};
+  volatile double *pv = P->part;
+  for (int bb = 0; bb < nb; bb++)
+    for (int k = 0; k < 4; k++) tot[k] += pv[(size_t)bb * kPartStride + k];
+  P->counter[1] = 0;
+  for (int k = 0; k < 4; k++) P->bcde[k] = tot[k];
+  finalize_iteration(B, P, K, src_max_norm[p]);
+}
+
+// ----------------------------------------------------- association export
+// Rows of the last association as (original row, original column, value),
+// written into a compact buffer at row offsets computed on the host.
+__global__ void k_export(const PairDev *P, const int *row_start, int *cols, float *vals, const int *tperm) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= P->n) return;
+  int z = P->nnz_row[s];
+  int o = row_start[s];
+  for (int c = 0; c < z; c++) {
+    cols[o + c] = tperm[P->A_j[(size_t)c * P->n + s]];
+    vals[o + c] = P->A_v[(size_t)c * P->n + s];
+  }
+}
+
+// --------------------------------------------------------- template dispatch
+using AssocFn = void (*)(BatchDev, KParams);
+using OvfFn = void (*)(BatchDev, KParams);
+
+template <int FCH, int LCH, bool GT>
+void pick(AssocFn &a, OvfFn &o) {
+  a = k_assoc<FCH, LCH, GT>;
+  o = k_overflow<FCH, LCH, GT>;
+}
+
+int select_kernels(const KParams &K, int F, int C, AssocFn &a, OvfFn &o) {
+  int fch = K.use_int ? (F + 3) / 4 : 0;
+  int lch = K.use_sem ? (C + 3) / 4 : 0;
+  bool gt = K.use_gtype != 0;
+  if (fch > 2 || lch > 9) return CVO_ERR_UNSUPPORTED;
+  if (lch > 0 && lch <= 5) lch = 5;
+  else if (lch > 5) lch = 9;
+#define CVO_PICK(FC, LC)                         \
+  if (fch == FC && lch == LC) {                  \
+    if (gt) pick<FC, LC, true>(a, o);            \
+    else pick<FC, LC, false>(a, o);              \
+    return 0;                                    \
+  }
+  CVO_PICK(0, 0) CVO_PICK(1, 0) CVO_PICK(2, 0)
+  CVO_PICK(0, 5) CVO_PICK(1, 5) CVO_PICK(2, 5)
+  CVO_PICK(0, 9) CVO_PICK(1, 9) CVO_PICK(2, 9)
+#undef CVO_PICK
+  return CVO_ERR_UNSUPPORTED;
+}
+
+// ------------------------------------------------------------ device arena
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0, off = 0;
+  template <typename T>
+  T *take(size_t count) {
+    size_t bytes = (sizeof(T) * std::max<size_t>(count, 1) + 255) & ~(size_t)255;
+    T *p = reinterpret_cast<T *>(base + off);
+    off += bytes;
+    return p;
+  }
+};
+
+}  // namespace
+
+struct Workspace {
+  char *dev = nullptr;
+  size_t dev_cap = 0;
+  int *pinned = nullptr;
+};
+
+static int ensure_workspace(Handle *h, size_t bytes) {
+  if (!h->ws) h->ws = new Workspace();
+  Workspace *w = h->ws;
+  if (!w->pinned) CVO_CUDA_TRY(h, cudaMallocHost((void **)&w->pinned, 4096));
+  if (w->dev_cap >= bytes) return 0;
+  if (w->dev) { cudaStreamSynchronize(h->stream); cudaFree(w->dev); w->dev = nullptr; w->dev_cap = 0; }
+  size_t want = bytes + bytes / 4 + (1 << 20);
+  cudaError_t e = cudaMalloc((void **)&w->dev, want);
+  if (e != cudaSuccess) {
+    set_cuda_error(h, e, "workspace");
+    return e == cudaErrorMemoryAllocation ? CVO_ERR_OUT_OF_MEMORY : CVO_ERR_CUDA;
+  }
+  w->dev_cap = want;
+  return 0;
+}
+
+void free_workspace(Handle *h) {
+  if (!h->ws) return;
+  if (h->ws->dev) cudaFree(h->ws->dev);
+  if (h->ws->pinned) cudaFreeHost(h->ws->pinned);
+  delete h->ws;
+  h->ws = nullptr;
+}
+
+KParams make_kparams(const cvo_params &p) {
+  KParams k;
+  memset(&k, 0, sizeof(k));
+  k.sigma2 = p.sigma * p.sigma;
+  k.c2 = p.c_ell * p.c_ell;
+  k.c_sigma2 = p.c_sigma * p.c_sigma;
+  k.s_ell = p.s_ell;
+  k.s_sigma2 = p.s_sigma * p.s_sigma;
+  k.s_sigma_sq = p.s_sigma * p.s_sigma;
+  k.sp_thres = p.sp_thres;
+  k.log_geo = logf(p.sp_thres / k.sigma2);
+  k.d2_c_thres = 1.f;
+  k.d2_s_thres = 1.f;
+  if (p.is_using_intensity) k.d2_c_thres = (float)(-2.0 * (double)k.c2 * (double)logf(p.sp_thres / k.c_sigma2));
+  if (p.is_using_semantics)
+    k.d2_s_thres = (float)(-2.0 * (double)k.s_ell * (double)k.s_ell * (double)logf(p.sp_thres / k.s_sigma2));
+  k.c = p.c; k.d = p.d;
+  k.eps = p.eps; k.eps_2 = p.eps_2; k.min_step = p.min_step; k.max_step = p.max_step;
+  k.ell_decay_rate = p.ell_decay_rate; k.ell_min = p.ell_min;
+  k.indicator_stable_threshold = p.indicator_stable_threshold;
+  k.ell_decay_start = p.ell_decay_start;
+  k.indicator_window_size = p.indicator_window_size;
+  k.max_iter = p.MAX_ITER;
+  k.nn_max = p.nearest_neighbors_max;
+  k.use_range_ell_step = p.is_using_range_ell;
+  k.use_geo = p.is_using_geometry;
+  k.use_int = p.is_using_intensity;
+  k.use_sem = p.is_using_semantics;
+  k.use_gtype = p.is_using_geometric_type;
+  k.cell_mult = 1.0f;
+  return k;
+}
+
+static float host_range_ell(float ell, float dist) { return (float)(((double)dist / 500.0 + 1.0) * (double)ell); }
+static float host_radius(const KParams &K, float ell, float norm) {
+  if (!K.use_geo) return INFINITY;
+  float l = host_range_ell(ell, norm);
+  float d2t = (float)(-2.0 * (double)l * (double)l * (double)K.log_geo);
+  return std::sqrt(std::max(d2t, 0.f));
+}
+
+// ------------------------------------------------------------ batch setup
+namespace {
+
+struct BatchHost {
+  BatchDev B;
+  std::vector<PairDev> pairs;
+  std::vector<int> tile_off, row_off, tgt_off, rblk_off, sblk_off;
+  float *src_max_norm = nullptr;
+  AssocFn assoc = nullptr;
+  OvfFn ovf = nullptr;
+  int assoc_blocks = 0, ovf_blocks = 0, xform_blocks = 0;
+};
+
+// Lays out every device buffer of a batch in the handle's workspace.
+int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                const std::vector<float> &T_init, int mode, int capmax, const std::vector<float> &ell0,
+                BatchHost *bh) {
+  const int np = (int)srcs.size();
+  int F = srcs[0]->F, C = srcs[0]->C;
+  for (int p = 0; p < np; p++) {
+    if (srcs[p]->F != F || tgts[p]->F != F || srcs[p]->C != C || tgts[p]->C != C) return CVO_ERR_INVALID_ARG;
+    if (K.use_gtype && (!srcs[p]->has_geo || !tgts[p]->has_geo)) return CVO_ERR_INVALID_ARG;
+  }
+  int rc = select_kernels(K, F, C, bh->assoc, bh->ovf);
+  if (rc) return rc;
+  // grid levels per pair
+  std::vector<std::vector<GridDesc>> lv(np);
+  std::vector<std::vector<float>> lr(np);
+  for (int p = 0; p < np; p++) {
+    DevCloud *t = tgts[p];
+    float cm = K.cell_mult;
+    std::vector<int> exps;
+    if (!K.use_geo) {
+      exps.push_back(1000);
+    } else {
+      float ell_hi = ell0[p];
+      float ell_lo = (mode == MODE_ALIGN) ? std::min(K.ell_min, ell_hi) : ell_hi;
+      float r_hi = host_radius(K, ell_hi, srcs[p]->max_norm);
+      float r_lo = host_radius(K, ell_lo, 0.f);
+      int e_hi = level_for_radius(cm * r_hi), e_lo = level_for_radius(cm * r_lo);
+      if (e_hi - e_lo + 1 > 24) e_lo = e_hi - 23;
+      for (int e = e_lo; e <= e_hi; e++) exps.push_back(e);
+    }
+    for (int e : exps) {
+      GridDesc g;
+      if ((rc = cloud_level(h, t, e, &g))) return rc;
+      lv[p].push_back(g);
+      lr[p].push_back(e >= 1000 ? INFINITY : (float)(g.h / cm));
+    }
+  }
+  // sizes
+  bh->tile_off.assign(np + 1, 0);
+  bh->row_off.assign(np + 1, 0);
+  bh->tgt_off.assign(np + 1, 0);
+  bh->rblk_off.assign(np + 1, 0);
+  bh->sblk_off.assign(np + 1, 0);
+  size_t bytes = 0;
+  auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
+  int max_part_blocks = 0;
+  for (int p = 0; p < np; p++) {
+    int n = srcs[p]->n, m = tgts[p]->n;
+    bh->tile_off[p + 1] = bh->tile_off[p] + (n + 31) / 32;
+    bh->row_off[p + 1] = bh->row_off[p] + n;
+    bh->tgt_off[p + 1] = bh->tgt_off[p] + m;
+    int rb = (n + kReduceRows - 1) / kReduceRows, sb = (n + kStepThreads - 1) / kStepThreads;
+    bh->rblk_off[p + 1] = bh->rblk_off[p] + rb;
+    bh->sblk_off[p + 1] = bh->sblk_off[p] + sb;
+    max_part_blocks = std::max(max_part_blocks, std::max(rb, sb));
+    add(sizeof(float4) * m);                                     // ycur
+    if (mode != MODE_IP) { add(sizeof(int) * (size_t)n * capmax); add(sizeof(float) * (size_t)n * capmax); }
+    add(sizeof(int) * n);                                        // nnz_row
+    add(sizeof(float) * 8 * (size_t)n);                          // row_sums
+    add(sizeof(double) * kPartStride * (size_t)std::max(rb, sb)); // partials
+    add(sizeof(unsigned) * 2);
+    add(sizeof(GridDesc) * lv[p].size());
+  }
+  const int total_rows = bh->row_off[np];
+  add(sizeof(PairDev) * np);
+  add(sizeof(int) * (np + 1) * 5);
+  add(sizeof(OvfEntry) * std::max(total_rows, 1));
+  add(sizeof(int) * 4);
+  add(sizeof(float) * np);
+  if ((rc = ensure_workspace(h, bytes))) return rc;
+  Arena ar;
+  ar.base = h->ws->dev;
+  ar.cap = h->ws->dev_cap;
+  bh->pairs.assign(np, PairDev());
+  std::vector<GridDesc *> lvdev(np);
+  std::vector<std::pair<void *, std::pair<const void *, size_t>>> uploads;
+  for (int p = 0; p < np; p++) {
+    PairDev &P = bh->pairs[p];
+    memset(&P, 0, sizeof(P));
+    DevCloud *s = srcs[p], *t = tgts[p];
+    P.n = s->n; P.m = t->n; P.F = F; P.C = C;
+    P.xs = s->spos; P.xf = s->sfeat; P.xl = s->slab; P.xg = s->sgeo; P.sperm = s->sperm;
+    P.ycur = ar.take<float4>(t->n);
+    if (mode != MODE_IP) { P.A_j = ar.take<int>((size_t)s->n * capmax); P.A_v = ar.take<float>((size_t)s->n * capmax); }
+    P.nnz_row = ar.take<int>(s->n);
+    P.row_sums = ar.take<float>(8 * (size_t)s->n);
+    int rb = bh->rblk_off[p + 1] - bh->rblk_off[p], sb = bh->sblk_off[p + 1] - bh->sblk_off[p];
+    P.part = ar.take<double>(kPartStride * (size_t)std::max(rb, sb));
+    P.counter = ar.take<unsigned>(2);
+    lvdev[p] = ar.take<GridDesc>(lv[p].size());
+    uploads.push_back({lvdev[p], {lv[p].data(), sizeof(GridDesc) * lv[p].size()}});
+    P.levels = lvdev[p];
+    P.nlevels = (int)lv[p].size();
+    for (int i = 0; i < P.nlevels && i < 24; i++) P.level_r[i] = lr[p][i];
+    P.capmax = capmax;
+    P.mode = mode;
+    for (int r = 0; r < 3; r++) {
+      for (int c = 0; c < 3; c++) P.R[3 * r + c] = T_init[16 * p + c * 4 + r];
+      P.T[r] = T_init[16 * p + 12 + r];
+    }
+    // target transform R^T, -R^T T (canonical order)
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) P.Ri[3 * r + c] = P.R[3 * c + r];
+    for (int r = 0; r < 3; r++) {
+      float a = P.Ri[3 * r] * P.T[0], b = P.Ri[3 * r + 1] * P.T[1], c = P.Ri[3 * r + 2] * P.T[2];
+      P.Ti[r] = -((a + b) + c);
+    }
+    P.ell = ell0[p];
+    P.cap = capmax;
+    // initial level
+    float r0 = host_radius(K, P.ell, s->max_norm);
+    P.level = P.nlevels - 1;
+    for (int i = 0; i < P.nlevels; i++)
+      if (P.level_r[i] >= r0) { P.level = i; break; }
+    P.level_used = P.level;
+    P.rq_max = r0;
+    P.done = (s->n == 0 || t->n == 0) ? 1 : 0;
+  }
+  PairDev *pairs_d = ar.take<PairDev>(np);
+  int *offs_d = ar.take<int>((size_t)(np + 1) * 5);
+  OvfEntry *ovf_d = ar.take<OvfEntry>(std::max(total_rows, 1));
+  int *ctr_d = ar.take<int>(4);
+  bh->src_max_norm = ar.take<float>(np);
+  // zero counters of every pair
+  for (int p = 0; p < np; p++) CVO_CUDA_TRY(h, cudaMemsetAsync(bh->pairs[p].counter, 0, 2 * sizeof(unsigned), h->stream));
+  for (auto &u : uploads) CVO_CUDA_TRY(h, cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, h->stream));
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(pairs_d, bh->pairs.data(), sizeof(PairDev) * np, cudaMemcpyHostToDevice, h->stream));
+  std::vector<int> offs;
+  for (auto *v : {&bh->tile_off, &bh->row_off, &bh->tgt_off, &bh->rblk_off, &bh->sblk_off}) offs.insert(offs.end(), v->begin(), v->end());
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(offs_d, offs.data(), sizeof(int) * offs.size(), cudaMemcpyHostToDevice, h->stream));
+  std::vector<float> mn(np);
+  int active = 0;
+  for (int p = 0; p < np; p++) { mn[p] = srcs[p]->max_norm; if (!bh->pairs[p].done) active++; }
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(bh->src_max_norm, mn.data(), sizeof(float) * np, cudaMemcpyHostToDevice, h->stream));
+  int ctr_h[4] = {0, 0, active, 0};
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(ctr_d, ctr_h, sizeof(ctr_h), cudaMemcpyHostToDevice, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  BatchDev &B = bh->B;
+  memset(&B, 0, sizeof(B));
+  B.npairs = np;
+  B.total_warps = bh->tile_off[np];
+  B.total_rows = total_rows;
+  B.total_targets = bh->tgt_off[np];
+  B.pairs = pairs_d;
+  B.tile_off = offs_d;
+  B.row_off = offs_d + (np + 1);
+  B.tgt_off = offs_d + 2 * (np + 1);
+  B.rblk_off = offs_d + 3 * (np + 1);
+  B.sblk_off = offs_d + 4 * (np + 1);
+  B.total_rblocks = bh->rblk_off[np];
+  B.total_sblocks = bh->sblk_off[np];
+  B.ovf = ovf_d;
+  B.ovf_n = ctr_d;
+  B.ovf_cap = std::max(total_rows, 1);
+  B.err = ctr_d + 1;
+  B.active = ctr_d + 2;
+  bh->assoc_blocks = (B.total_warps * 32 + kAssocThreads - 1) / kAssocThreads;
+  bh->xform_blocks = (B.total_targets + 255) / 256;
+  bh->ovf_blocks = std::max(1, h->num_sms * 4);
+  return 0;
+}
+
+void launch_association(Handle *h, BatchHost *bh, const KParams &K) {
+  BatchDev &B = bh->B;
+  k_transform<<<std::max(bh->xform_blocks, 1), 256, 0, h->stream>>>(B);
+  bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, 0, h->stream>>>(B, K);
+  bh->ovf<<<bh->ovf_blocks, kOvfThreads, 0, h->stream>>>(B, K);
+  k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
+  h->launches += 4;
+}
+
+void launch_iteration(Handle *h, BatchHost *bh, const KParams &K) {
+  launch_association(h, bh, K);
+  k_step<<<std::max(bh->B.total_sblocks, 1), kStepThreads, 0, h->stream>>>(bh->B, K, bh->src_max_norm);
+  h->launches += 1;
+}
+
+int read_pairs(Handle *h, BatchHost *bh) {
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(bh->pairs.data(), bh->B.pairs, sizeof(PairDev) * bh->B.npairs,
+                                  cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int check_err(Handle *h, BatchHost *bh) {
+  int e = 0;
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(&e, bh->B.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return e ? e : 0;
+}
+
+// Exports the association of pair p into per-row CSR on the host (rows =
+// original source indices, columns ascending).
+int export_pair(Handle *h, BatchHost *bh, int p, DevCloud *src, DevCloud *tgt, std::vector<int> *rowptr,
+                std::vector<int> *cols, std::vector<float> *vals) {
+  PairDev &P = bh->pairs[p];
+  int n = P.n;
+  std::vector<int> nnz(n);
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(nnz.data(), P.nnz_row, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<int> sperm(n);
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(sperm.data(), src->sperm, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  std::vector<int> start(n + 1, 0);
+  for (int s = 0; s < n; s++) start[s + 1] = start[s] + nnz[s];
+  int total = start[n];
+  int *start_d = nullptr, *cols_d = nullptr;
+  float *vals_d = nullptr;
+  CVO_CUDA_TRY(h, cudaMalloc((void **)&start_d, sizeof(int) * (n + 1)));
+  CVO_CUDA_TRY(h, cudaMalloc((void **)&cols_d, sizeof(int) * std::max(total, 1)));
+  CVO_CUDA_TRY(h, cudaMalloc((void **)&vals_d, sizeof(float) * std::max(total, 1)));
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(start_d, start.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
+  GridDesc g = tgt->levels_host.begin()->second;
+  {
+    // level used by the last association of this pair
+    std::vector<GridDesc> lv(P.nlevels);
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(lv.data(), P.levels, sizeof(GridDesc) * P.nlevels, cudaMemcpyDeviceToHost, h->stream));
+    CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    g = lv[P.level_used];
+  }
+  PairDev *pd = bh->B.pairs + p;
+  k_export<<<(n + 255) / 256, 256, 0, h->stream>>>(pd, start_d, cols_d, vals_d, g.perm);
+  h->launches++;
+  std::vector<int> c(total);
+  std::vector<float> v(total);
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(c.data(), cols_d, sizeof(int) * total, cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(v.data(), vals_d, sizeof(float) * total, cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  cudaFree(start_d); cudaFree(cols_d); cudaFree(vals_d);
+  // reorder rows to original order and sort columns
+  std::vector<int> cnt(n, 0);
+  for (int s = 0; s < n; s++) cnt[sperm[s]] = nnz[s];
+  rowptr->assign(n + 1, 0);
+  for (int i = 0; i < n; i++) (*rowptr)[i + 1] = (*rowptr)[i] + cnt[i];
+  cols->assign(total, 0);
+  vals->assign(total, 0.f);
+  std::vector<std::pair<int, float>> tmp;
+  for (int s = 0; s < n; s++) {
+    int i = sperm[s];
+    tmp.clear();
+    for (int k = start[s]; k < start[s + 1]; k++) tmp.push_back({c[k], v[k]});
+    std::sort(tmp.begin(), tmp.end(), [](const std::pair<int, float> &a, const std::pair<int, float> &b) { return a.first < b.first; });
+    int o = (*rowptr)[i];
+    for (size_t k = 0; k < tmp.size(); k++) { (*cols)[o + k] = tmp[k].first; (*vals)[o + k] = tmp[k].second; }
+  }
+  return 0;
+}
+
+}  // namespace
+
+// Runs the align loop for every pair of the batch until all pairs stop.
+int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                    const std::vector<float> &T_init, BatchResult *res, double *secs, bool export_assoc,
+                    std::vector<std::vector<int>> *a_rows, std::vector<std::vector<int>> *a_cols,
+                    std::vector<std::vector<float>> *a_vals) {
+  const int np = (int)srcs.size();
+  if (np == 0) return 0;
+  KParams K = make_kparams(h->params);
+  if (K.indicator_window_size > kMaxIndicatorWindow || K.indicator_window_size < 1) return CVO_ERR_UNSUPPORTED;
+  int capmax = std::max(h->params.nearest_neighbors_max, 0);
+  BatchHost bh;
+  std::vector<float> ell0(np, h->params.ell_init);
+  int rc = build_batch(h, K, srcs, tgts, T_init, MODE_ALIGN, capmax, ell0, &bh);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, h->stream);
+  // capture one chunk of iterations as a CUDA graph and relaunch it
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long before = h->launches;
+  CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int it = 0; it < kChunk; it++) launch_iteration(h, &bh, K);
+  CVO_CUDA_TRY(h, cudaStreamEndCapture(h->stream, &graph));
+  long long per_chunk = h->launches - before;
+  h->launches = before;
+  CVO_CUDA_TRY(h, cudaGraphInstantiate(&exec, graph, 0));
+  int *active_h = h->ws->pinned;
+  long long max_chunks = (long long)h->params.MAX_ITER / kChunk + 2;
+  for (long long ch = 0; ch < max_chunks; ch++) {
+    CVO_CUDA_TRY(h, cudaGraphLaunch(exec, h->stream));
+    h->launches += per_chunk;
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(active_h, bh.B.active, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (*active_h <= 0) break;
+  }
+  cudaEventRecord(e1, h->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  if (secs) *secs = ms / 1000.0;
+  if ((rc = check_err(h, &bh))) return rc;
+  if ((rc = read_pairs(h, &bh))) return rc;
+  res->T_out.assign(16 * np, 0.f);
+  res->ret.assign(np, 0);
+  res->iters.assign(np, 0);
+  res->asum.assign(np, 0.0);
+  res->nnz.assign(np, 0);
+  for (int p = 0; p < np; p++) {
+    PairDev &P = bh.pairs[p];
+    float *T = &res->T_out[16 * p];
+    for (int r = 0; r < 3; r++) {
+      for (int c = 0; c < 3; c++) T[c * 4 + r] = P.R[3 * c + r];
+      float a = P.R[r] * P.T[0], b = P.R[3 + r] * P.T[1], c = P.R[6 + r] * P.T[2];
+      T[12 + r] = -((a + b) + c);
+    }
+    T[15] = 1.f;
+    res->ret[p] = P.ret;
+    res->iters[p] = P.iter;
+    res->asum[p] = P.asum;
+    res->nnz[p] = P.nnz_sum;
+    if (srcs[p]->n == 0 || tgts[p]->n == 0) {
+      for (int t = 0; t < 16; t++) T[t] = (t % 5 == 0) ? 1.f : 0.f;
+      for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T[c * 4 + r] = T_init[16 * p + r * 4 + c]; }
+    }
+  }
+  if (export_assoc && a_rows) {
+    a_rows->resize(np); a_cols->resize(np); a_vals->resize(np);
+    for (int p = 0; p < np; p++)
+      if ((rc = export_pair(h, &bh, p, srcs[p], tgts[p], &(*a_rows)[p], &(*a_cols)[p], &(*a_vals)[p]))) return rc;
+  }
+  return 0;
+}
+
+// One association pass (no iteration) of one source/target pair under each of
+// the given poses (inner_product_impl, src/cvo/CvoGPU.cu:1673-1732).
+int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::vector<float> &T, float ell, int cap,
+                            std::vector<double> *asum, std::vector<long long> *nnz, bool export_assoc,
+                            std::vector<int> *a_rowptr, std::vector<int> *a_cols, std::vector<float> *a_vals) {
+  const int np = (int)(T.size() / 16);
+  KParams K = make_kparams(h->params);
+  BatchHost bh;
+  std::vector<DevCloud *> srcs(np, src), tgts(np, tgt);
+  std::vector<float> ell0(np, ell);
+  int rc = build_batch(h, K, srcs, tgts, T, export_assoc ? MODE_EXPORT : MODE_IP, std::max(cap, 0), ell0, &bh);
+  if (rc) return rc;
+  launch_association(h, &bh, K);
+  if ((rc = check_err(h, &bh))) return rc;
+  if ((rc = read_pairs(h, &bh))) return rc;
+  asum->assign(np, 0.0);
+  nnz->assign(np, 0);
+  for (int p = 0; p < np; p++) { (*asum)[p] = bh.pairs[p].asum; (*nnz)[p] = bh.pairs[p].nnz_sum; }
+  if (export_assoc && np == 1)
+    if ((rc = export_pair(h, &bh, 0, src, tgt, a_rowptr, a_cols, a_vals))) return rc;
+  return 0;
+}
+
+int set_cuda_error(Handle *h, cudaError_t e, const char *where) {
+  if (h) {
+    h->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  }
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? CVO_ERR_OUT_OF_MEMORY : CVO_ERR_CUDA;
+}
+
+}  // namespace cvo_gb

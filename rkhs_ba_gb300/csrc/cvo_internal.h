@@ -1,0 +1,201 @@
+// cvo_internal.h -- internal types shared by the CUDA translation units.
+//
+// Data layout in HBM (replaces the reference's 176-240 B AoS CvoPoint records,
+// include/UnifiedCvo/utils/PointSegmentedDistribution.hpp:51-144):
+//   positions : float4 {x, y, z, w}   (w = ||p|| for sources, original index bits for targets)
+//   features  : n * FP floats, FP = F rounded up to 4 (float4 loads)
+//   labels    : n * CP floats, CP = C rounded up to 4
+//   geom_type : float2
+// A source cloud is additionally kept in "tile order" (Morton order, 32 points per
+// warp tile); a target cloud keeps one spatial-hash grid per cell size ("level").
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <map>
+#include "../../include/cvo_gb300.h"
+
+namespace cvo_gb {
+
+constexpr int kWarp = 32;
+constexpr int kMaxIndicatorWindow = 128;
+constexpr int kHist1Bits = 11;              // overflow radix-select, first digit
+constexpr int kMaxTargetBits = 22;          // targets per cloud <= 4M
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+
+// ------------------------------------------------------------------ grid
+// One spatial-hash grid over a target cloud at cell size h.  Cells are keyed by
+// integer coordinates relative to the cloud's bounding-box minimum; the table
+// uses linear probing.  Points are stored sorted by (table slot, original index),
+// so the members of one cell are contiguous and in ascending original index.
+struct GridDesc {
+  float h, inv_h;
+  float ox, oy, oz;
+  int dimx, dimy, dimz;         // number of cells per axis over the bounding box
+  int tbits;                    // table size = 1 << tbits
+  const unsigned long long *keys;
+  const int *cstart;
+  const int *ccount;
+  const int *perm;              // sorted position -> original index
+  const float4 *pos;            // sorted copy: x, y, z, original index (int bits)
+  const float *feat;            // sorted copy, n * FP
+  const float *lab;             // sorted copy, n * CP
+  const float2 *geo;            // sorted copy (may be null)
+};
+
+struct DevCloud {
+  int n = 0, F = 0, C = 0, FP = 0, CP = 0;
+  bool has_geo = false;
+  float bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
+  float max_norm = 0.f;
+  // original order
+  float4 *pos = nullptr;
+  float *feat = nullptr;
+  float *lab = nullptr;
+  float2 *geo = nullptr;
+  // source tile order
+  int *sperm = nullptr;
+  float4 *spos = nullptr;
+  float *sfeat = nullptr;
+  float *slab = nullptr;
+  float2 *sgeo = nullptr;
+  // target grids keyed by quantised cell-size exponent
+  std::map<int, GridDesc *> levels_dev;   // device copies of descriptors
+  std::map<int, GridDesc> levels_host;
+  std::vector<void *> level_allocs;
+};
+
+// ----------------------------------------------------------- kernel params
+// Per-call kernel constants (identical for all pairs of a batch).
+struct KParams {
+  float sigma2, c2, c_sigma2, s_ell, s_sigma2, s_sigma_sq, sp_thres;
+  float log_geo;         // logf(sp_thres / sigma2), evaluated on the host
+  float d2_c_thres, d2_s_thres;
+  float c, d;            // so(3) / R^3 inner-product scales
+  float eps, eps_2, min_step, max_step;
+  float ell_decay_rate, ell_min, indicator_stable_threshold;
+  int ell_decay_start, indicator_window_size, max_iter, nn_max, use_range_ell_step;
+  int use_geo, use_int, use_sem, use_gtype;
+  float cell_mult;       // cell size >= cell_mult * search radius
+};
+
+// Per-pair device state.  One struct per pair, in device memory.
+struct PairDev {
+  // problem
+  int n, m;                       // source rows, target points
+  const float4 *xs;               // source, tile order (x,y,z,||x||)
+  const float *xf, *xl;
+  const float2 *xg;
+  const int *sperm;
+  const GridDesc *levels;         // device array of grid levels of the target
+  int nlevels;
+  float level_r[24];              // largest search radius each level serves
+  float4 *ycur;                   // transformed targets, current level order
+  int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s]
+  int *nnz_row;                   // n
+  float *row_sums;                // n * 8: omega(3)/c, v(3)/d, asum, count
+  double *part;                   // reduce partials
+  unsigned int *counter;          // last-block counters [2]
+  int F, C;                       // feature / label dimensions (source and target agree)
+  int capmax;
+  int mode;                       // 0 align, 1 inner product, 2 export
+  // iteration state
+  float R[9], T[3];               // internal pose
+  float Ri[9], Ti[3];             // target transform R^T, -R^T T
+  float ell;
+  int cap;
+  int level, level_used;
+  int iter, done, ret;
+  float xi[6];
+  double grad[6];
+  double asum;
+  long long nnz_sum;
+  int max_row;
+  double bcde[4];
+  double step, dist;
+  float rq_max;                   // largest search radius of this iteration
+  // indicator queues (ring buffers)
+  float qs[kMaxIndicatorWindow], qe[kMaxIndicatorWindow];
+  int qs_head, qs_len, qe_head, qe_len;
+  float ssum, esum;
+};
+
+struct OvfEntry { int pair; int row; };
+
+// Batch of pairs processed together by every kernel launch.
+struct BatchDev {
+  int npairs;
+  int total_warps;                // association tiles over all pairs
+  int total_rows;                 // sum of n
+  int total_targets;              // sum of m
+  PairDev *pairs;                 // device array
+  const int *tile_off;            // npairs + 1 (prefix of tile counts)
+  const int *row_off;             // npairs + 1 (prefix of n)
+  const int *tgt_off;             // npairs + 1 (prefix of m)
+  OvfEntry *ovf;                  // overflow list
+  int *ovf_n;                     // overflow count (reset by the transform kernel)
+  int ovf_cap;
+  int *err;                       // error word (0 ok)
+  const int *rblk_off;            // reduce blocks per pair (prefix)
+  const int *sblk_off;            // step blocks per pair (prefix)
+  int total_rblocks, total_sblocks;
+  int *active;                    // number of pairs not done
+};
+
+// ------------------------------------------------------------- host side
+struct Workspace;
+
+struct Handle {
+  cvo_params params;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int num_sms = 0;
+  long long launches = 0;
+  std::string last_error;
+  Workspace *ws = nullptr;
+};
+
+// grid / cloud management (cvo_grid.cu)
+int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out);
+void cloud_free(DevCloud *c);
+int cloud_level(Handle *h, DevCloud *c, int level_exp, GridDesc *host_desc);
+float level_cell_size(int level_exp);
+int level_for_radius(float r);
+
+// radix sort / scan (cvo_sort.cu)
+int radix_sort_pairs(Handle *h, unsigned int *keys, int *vals, unsigned int *keys_tmp, int *vals_tmp,
+                     int n, int key_bits);
+void exclusive_scan_int(Handle *h, const int *in, int *out, int n, int *scratch, int scratch_n);
+size_t scan_scratch_ints(int n);
+
+// engine (cvo_engine.cu)
+KParams make_kparams(const cvo_params &p);
+struct BatchResult {
+  std::vector<float> T_out;     // 16 per pair, column-major [R^T, -R^T T]
+  std::vector<int> ret, iters;
+  std::vector<double> asum;
+  std::vector<long long> nnz;
+};
+int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                    const std::vector<float> &T_init, BatchResult *res, double *secs,
+                    bool export_assoc, std::vector<std::vector<int>> *a_rows,
+                    std::vector<std::vector<int>> *a_cols, std::vector<std::vector<float>> *a_vals);
+int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::vector<float> &T, float ell,
+                            int cap, std::vector<double> *asum, std::vector<long long> *nnz,
+                            bool export_assoc, std::vector<int> *a_rowptr_host, std::vector<int> *a_cols,
+                            std::vector<float> *a_vals);
+
+// IRLS (cvo_irls.cu)
+int run_align_multi(Handle *h, int n_frames, DevCloud *const *clouds, double *poses, const uint8_t *hold_const,
+                    int n_edges, const int *edges, double *secs, int *iters);
+
+// error helpers
+int set_cuda_error(Handle *h, cudaError_t e, const char *where);
+#define CVO_CUDA_TRY(h, call)                                      \
+  do {                                                             \
+    cudaError_t e__ = (call);                                      \
+    if (e__ != cudaSuccess) return set_cuda_error((h), e__, #call); \
+  } while (0)
+
+}  // namespace cvo_gb

@@ -1,0 +1,357 @@
+"""``CvoGPU``: the Python mirror of the reference's ``cvo::CvoGPU`` class.
+
+Method names, argument meaning, pose conventions and return codes follow
+include/UnifiedCvo/cvo/CvoGPU.hpp:43-274; every call goes through the C ABI of
+the native library (include/cvo_gb300.h).  4x4 matrices are numpy arrays in
+the usual row-major (4, 4) shape; they are passed to the library column-major.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .cloud import CvoPointCloud
+
+_FP = C.POINTER(C.c_float)
+
+
+def _m16(T) -> np.ndarray:
+    T = np.asarray(T, dtype=np.float32).reshape(4, 4)
+    return np.ascontiguousarray(T.T.reshape(16))
+
+
+def _from16(a) -> np.ndarray:
+    return np.asarray(a, dtype=np.float32).reshape(4, 4).T.copy()
+
+
+class CvoParams:
+    """cvo::CvoParams (include/UnifiedCvo/cvo/CvoParams.hpp:12-136) as attributes."""
+
+    def __init__(self, yaml_path: str | None = None):
+        self._c = L.CvoParamsC()
+        L.lib().cvo_params_default(C.byref(self._c))
+        if yaml_path is not None:
+            self.read_yaml(yaml_path)
+
+    def read_yaml(self, path: str) -> "CvoParams":
+        L.check(L.lib().cvo_params_read_yaml(path.encode(), C.byref(self._c)), "cvo_params_read_yaml")
+        return self
+
+    def __getattr__(self, k):
+        if k.startswith("_"):
+            raise AttributeError(k)
+        return getattr(self._c, k)
+
+    def __setattr__(self, k, v):
+        if k.startswith("_"):
+            object.__setattr__(self, k, v)
+        else:
+            if not any(k == f for f, _ in L.PARAM_FIELDS):
+                raise AttributeError("unknown CvoParams field %r" % k)
+            setattr(self._c, k, v)
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self._c, f) for f, _ in L.PARAM_FIELDS}
+
+    def copy(self) -> "CvoParams":
+        p = CvoParams()
+        C.memmove(C.byref(p._c), C.byref(self._c), C.sizeof(L.CvoParamsC))
+        return p
+
+
+@dataclass
+class Association:
+    """cvo::Association (include/UnifiedCvo/cvo/Association.hpp:5-12): CSR rows are
+    source indices, columns target indices."""
+    rows: int = 0
+    cols: int = 0
+    row_ptr: np.ndarray = field(default_factory=lambda: np.zeros(1, np.int64))
+    col: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    val: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    source_inliers: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    target_inliers: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+
+    @property
+    def nnz(self) -> int:
+        return int(self.col.shape[0])
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.row_ptr), shape=(self.rows, self.cols))
+
+
+@dataclass
+class CvoResultInfo:
+    """cvo::CvoResultInfo (include/UnifiedCvo/cvo/CvoGPU.hpp:34-40)."""
+    return_code: int
+    T_s2t: np.ndarray
+    association: Association | None
+    registration_seconds: float
+    num_iters: int
+
+
+class GpuCloud:
+    """A cloud resident on the GPU (CvoPointCloudGPU); freed with the object."""
+
+    def __init__(self, cvo: "CvoGPU", cloud: CvoPointCloud):
+        self._cvo = cvo
+        self.cloud = cloud
+        self._h = C.c_void_p()
+        cs = cloud.c_struct()
+        L.check(L.lib().cvo_cloud_upload(cvo._h, C.byref(cs), C.byref(self._h)), "cvo_cloud_upload", cvo._h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __len__(self):
+        return L.lib().cvo_cloud_size(self._h)
+
+    def free(self):
+        if self._h:
+            L.lib().cvo_cloud_free(self._cvo._h, self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _read_assoc(a) -> Association:
+    lib = L.lib()
+    rows, cols = C.c_int(), C.c_int()
+    nnz, ns, nt = C.c_int64(), C.c_int64(), C.c_int64()
+    lib.cvo_assoc_info(a, C.byref(rows), C.byref(cols), C.byref(nnz), C.byref(ns), C.byref(nt))
+    rp = np.zeros(rows.value + 1, np.int64)
+    col = np.zeros(nnz.value, np.int32)
+    val = np.zeros(nnz.value, np.float32)
+    si = np.zeros(ns.value, np.int32)
+    ti = np.zeros(nt.value, np.int32)
+    lib.cvo_assoc_copy(a, rp.ctypes.data_as(C.POINTER(C.c_int64)), col.ctypes.data_as(C.POINTER(C.c_int)),
+                       val.ctypes.data_as(_FP), si.ctypes.data_as(C.POINTER(C.c_int)),
+                       ti.ctypes.data_as(C.POINTER(C.c_int)))
+    return Association(rows.value, cols.value, rp, col, val, si, ti)
+
+
+class _AssocBuf:
+    def __init__(self):
+        self.h = C.c_void_p()
+        L.check(L.lib().cvo_assoc_create(C.byref(self.h)), "cvo_assoc_create")
+
+    def __del__(self):
+        if self.h:
+            L.lib().cvo_assoc_destroy(self.h)
+
+
+class CvoGPU:
+    """GB300-native drop-in for cvo::CvoGPU."""
+
+    def __init__(self, param_file: str | None = None, params: CvoParams | None = None):
+        self._h = C.c_void_p()
+        lib = L.lib()
+        if params is not None:
+            L.check(lib.cvo_create_with_params(C.byref(params._c), C.byref(self._h)), "cvo_create_with_params")
+        elif param_file is not None:
+            L.check(lib.cvo_create(param_file.encode(), C.byref(self._h)), "cvo_create")
+        else:
+            L.check(lib.cvo_create_with_params(C.byref(CvoParams()._c), C.byref(self._h)), "cvo_create_with_params")
+
+    def close(self):
+        if self._h:
+            L.lib().cvo_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- parameters -----------------------------------------------------
+    def get_params(self) -> CvoParams:
+        p = CvoParams()
+        L.check(L.lib().cvo_get_params(self._h, C.byref(p._c)), "cvo_get_params")
+        return p
+
+    def write_params(self, p: CvoParams) -> None:
+        L.check(L.lib().cvo_write_params(self._h, C.byref(p._c)), "cvo_write_params")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(L.lib().cvo_kernel_launch_count(self._h))
+
+    def upload(self, cloud: CvoPointCloud) -> GpuCloud:
+        return GpuCloud(self, cloud)
+
+    # -- two-view -------------------------------------------------------
+    def align(self, source, target, T_init, want_association: bool = False):
+        """int CvoGPU::align(src, tgt, T_target_frame_to_source_frame, T_out&, assoc*, secs*, iters*)
+        (src/cvo/CvoGPU.cu:1516-1563).  Returns (ret, T_out, association, seconds, iters);
+        T_init is the internal initial pose (callers pass init_guess.inverse())."""
+        T_out = np.zeros(16, np.float32)
+        secs = C.c_double(0)
+        iters = C.c_int(0)
+        ab = _AssocBuf() if want_association else None
+        Ti = _m16(T_init)
+        lib = L.lib()
+        if isinstance(source, GpuCloud):
+            rc = lib.cvo_align_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP),
+                                   T_out.ctypes.data_as(_FP), ab.h if ab else None, C.byref(secs), C.byref(iters))
+        else:
+            s, t = source.c_struct(), target.c_struct()
+            rc = lib.cvo_align(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), T_out.ctypes.data_as(_FP),
+                               ab.h if ab else None, C.byref(secs), C.byref(iters))
+        L.check(rc, "cvo_align", self._h)
+        assoc = _read_assoc(ab.h) if ab else None
+        return (0 if rc == L.CVO_OK else -1), _from16(T_out), assoc, secs.value, iters.value
+
+    def align_s2t(self, source: CvoPointCloud, target: CvoPointCloud, T_s2t, is_returning_association=False):
+        """CvoResultInfo CvoGPU::align(src, tgt, T_source_frame_to_target_frame, assoc)
+        (src/cvo/CvoGPU.cu:1566-1611)."""
+        T_out = np.zeros(16, np.float32)
+        secs = C.c_double(0)
+        iters = C.c_int(0)
+        ret = C.c_int(0)
+        ab = _AssocBuf() if is_returning_association else None
+        s, t = source.c_struct(), target.c_struct()
+        Ti = _m16(T_s2t)
+        L.check(L.lib().cvo_align_s2t(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), int(bool(ab)),
+                                      T_out.ctypes.data_as(_FP), ab.h if ab else None, C.byref(secs), C.byref(iters),
+                                      C.byref(ret)), "cvo_align_s2t", self._h)
+        return CvoResultInfo(ret.value, _from16(T_out), _read_assoc(ab.h) if ab else None, secs.value, iters.value)
+
+    def align_batch(self, sources, targets, T_inits):
+        """Batched two-view align of device clouds (one persistent batch)."""
+        n = len(sources)
+        S = (C.c_void_p * n)(*[s.handle.value for s in sources])
+        Tg = (C.c_void_p * n)(*[t.handle.value for t in targets])
+        Ti = np.ascontiguousarray(np.concatenate([_m16(T) for T in T_inits]).astype(np.float32))
+        To = np.zeros(16 * n, np.float32)
+        rets = np.zeros(n, np.int32)
+        its = np.zeros(n, np.int32)
+        secs = C.c_double(0)
+        L.check(L.lib().cvo_align_batch_dev(self._h, n, S, Tg, Ti.ctypes.data_as(_FP), To.ctypes.data_as(_FP),
+                                            rets.ctypes.data_as(C.POINTER(C.c_int)),
+                                            its.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs)),
+                "cvo_align_batch_dev", self._h)
+        return [_from16(To[16 * i:16 * i + 16]) for i in range(n)], rets, its, secs.value
+
+    # -- inner products -------------------------------------------------
+    def inner_product_gpu(self, source, target, T, ell: float) -> float:
+        out = C.c_float(0)
+        Ti = _m16(T)
+        lib = L.lib()
+        if isinstance(source, GpuCloud):
+            rc = lib.cvo_inner_product_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP),
+                                           float(ell), C.byref(out))
+        else:
+            s, t = source.c_struct(), target.c_struct()
+            rc = lib.cvo_inner_product(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), float(ell),
+                                       C.byref(out))
+        L.check(rc, "cvo_inner_product", self._h)
+        return out.value
+
+    def inner_product_batch(self, source: GpuCloud, target: GpuCloud, Ts, ell: float) -> np.ndarray:
+        n = len(Ts)
+        Ti = np.ascontiguousarray(np.concatenate([_m16(T) for T in Ts]).astype(np.float32))
+        out = np.zeros(n, np.float32)
+        L.check(L.lib().cvo_inner_product_batch_dev(self._h, source.handle, target.handle, n, Ti.ctypes.data_as(_FP),
+                                                    float(ell), out.ctypes.data_as(_FP)),
+                "cvo_inner_product_batch_dev", self._h)
+        return out
+
+    def inner_product_cpu(self, source: CvoPointCloud, target: CvoPointCloud, T, ell: float) -> float:
+        out = C.c_float(0)
+        s, t = source.c_struct(), target.c_struct()
+        Ti = _m16(T)
+        L.check(L.lib().cvo_inner_product_cpu(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), float(ell),
+                                              C.byref(out)), "cvo_inner_product_cpu", self._h)
+        return out.value
+
+    def function_angle(self, source: CvoPointCloud, target: CvoPointCloud, T, ell: float,
+                       is_approximate: bool = True, is_gpu: bool = True) -> float:
+        out = C.c_float(0)
+        s, t = source.c_struct(), target.c_struct()
+        Ti = _m16(T)
+        L.check(L.lib().cvo_function_angle(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), float(ell),
+                                           int(is_approximate), int(is_gpu), C.byref(out)),
+                "cvo_function_angle", self._h)
+        return out.value
+
+    def compute_association_gpu(self, source: CvoPointCloud, target: CvoPointCloud, T, ell: float) -> Association:
+        ab = _AssocBuf()
+        s, t = source.c_struct(), target.c_struct()
+        Ti = _m16(T)
+        L.check(L.lib().cvo_compute_association(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), float(ell),
+                                                ab.h), "cvo_compute_association", self._h)
+        return _read_assoc(ab.h)
+
+    # -- global registration --------------------------------------------
+    @staticmethod
+    def rotation_grid(grid_kind: int = 0, num_guess: int = 0) -> np.ndarray:
+        lib = L.lib()
+        n = lib.cvo_rotation_grid(grid_kind, num_guess, None, 0)
+        L.check(n, "cvo_rotation_grid")
+        out = np.zeros(9 * n, np.float32)
+        lib.cvo_rotation_grid(grid_kind, num_guess, out.ctypes.data_as(_FP), n)
+        return out.reshape(n, 3, 3)
+
+    def get_nearest_init_pose(self, source, target, init_guess_ell: float, num_guess: int = 0, grid_kind: int = 0):
+        """CvoGPU::get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398); returns (T, seconds)."""
+        T_out = np.zeros(16, np.float32)
+        secs = C.c_double(0)
+        lib = L.lib()
+        if isinstance(source, GpuCloud):
+            rc = lib.cvo_get_nearest_init_pose_dev(self._h, source.handle, target.handle, float(init_guess_ell),
+                                                   int(num_guess), int(grid_kind), T_out.ctypes.data_as(_FP),
+                                                   C.byref(secs))
+        else:
+            s, t = source.c_struct(), target.c_struct()
+            rc = lib.cvo_get_nearest_init_pose(self._h, C.byref(s), C.byref(t), float(init_guess_ell), int(num_guess),
+                                               int(grid_kind), T_out.ctypes.data_as(_FP), C.byref(secs))
+        L.check(rc, "cvo_get_nearest_init_pose", self._h)
+        return _from16(T_out), secs.value
+
+    def register_hypotheses(self, source: GpuCloud, target: GpuCloud, T_inits, judge_ell: float):
+        """Refine every hypothesis with the batched align and keep the best final cos-angle.
+        Returns (T_out, best_index, cos_values, seconds)."""
+        n = len(T_inits)
+        Ti = np.ascontiguousarray(np.concatenate([_m16(T) for T in T_inits]).astype(np.float32))
+        To = np.zeros(16, np.float32)
+        best = C.c_int(-1)
+        cos = np.zeros(n, np.float32)
+        secs = C.c_double(0)
+        L.check(L.lib().cvo_register_hypotheses_dev(self._h, source.handle, target.handle, n, Ti.ctypes.data_as(_FP),
+                                                    float(judge_ell), To.ctypes.data_as(_FP), C.byref(best),
+                                                    cos.ctypes.data_as(_FP), C.byref(secs)),
+                "cvo_register_hypotheses_dev", self._h)
+        return _from16(To), best.value, cos, secs.value
+
+    # -- multi-frame ----------------------------------------------------
+    def align_multi(self, clouds, poses, hold_const, edges):
+        """CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670).
+        poses: (n, 12) row-major 3x4 frame->world (updated copy returned)."""
+        n = len(clouds)
+        P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(n, 12).copy())
+        hc = np.ascontiguousarray(np.asarray(hold_const, np.uint8).reshape(n))
+        E = np.ascontiguousarray(np.asarray(edges, np.int32).reshape(-1, 2))
+        secs = C.c_double(0)
+        iters = C.c_int(0)
+        lib = L.lib()
+        if isinstance(clouds[0], GpuCloud):
+            arr = (C.c_void_p * n)(*[c.handle.value for c in clouds])
+            rc = lib.cvo_align_multi_dev(self._h, n, arr, P.ctypes.data_as(C.POINTER(C.c_double)),
+                                         hc.ctypes.data_as(C.POINTER(C.c_uint8)), E.shape[0],
+                                         E.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs), C.byref(iters))
+        else:
+            cs = (L.CvoCloudC * n)(*[c.c_struct() for c in clouds])
+            rc = lib.cvo_align_multi(self._h, n, cs, P.ctypes.data_as(C.POINTER(C.c_double)),
+                                     hc.ctypes.data_as(C.POINTER(C.c_uint8)), E.shape[0],
+                                     E.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs), C.byref(iters))
+        L.check(rc, "cvo_align_multi", self._h)
+        return P, secs.value, iters.value

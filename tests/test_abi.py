@@ -1,0 +1,134 @@
+"""The C-ABI library loads, exports every symbol of include/cvo_gb300.h, and its
+structures have the layout the header declares (no GPU needed)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from rkhs_ba_gb300 import CvoGPU, CvoParams, CvoPointCloud, params_path
+from rkhs_ba_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "cvo_gb300.h")
+
+
+def _declared():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(cvo_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_every_declared_symbol_is_exported_and_bound():
+    lib = L.lib()
+    names = _declared()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in L.SIGNATURES, "no ctypes binding for %s" % n
+
+
+def test_struct_layout_matches_header():
+    """Compile a probe with gcc that prints sizeof/offsetof of the header's structs."""
+    fields = [f for f, _ in L.PARAM_FIELDS]
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "cvo_gb300.h"', 'int main(void){',
+           'printf("%zu %zu\\n", sizeof(cvo_params), sizeof(cvo_cloud));']
+    for f in fields:
+        src.append('printf("%%zu\\n", offsetof(cvo_params, %s));' % f)
+    for f in ("n", "F", "C", "xyz_stride", "xyz", "features", "labels", "geom_type"):
+        src.append('printf("%%zu\\n", offsetof(cvo_cloud, %s));' % f)
+    src.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(src))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-I" + os.path.dirname(HEADER), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    vals = [int(v) for v in out]
+    assert vals[0] == C.sizeof(L.CvoParamsC)
+    assert vals[1] == C.sizeof(L.CvoCloudC)
+    for k, f in enumerate(fields):
+        assert vals[2 + k] == getattr(L.CvoParamsC, f).offset, f
+    for k, f in enumerate(("n", "F", "C", "xyz_stride", "xyz", "features", "labels", "geom_type")):
+        assert vals[2 + len(fields) + k] == getattr(L.CvoCloudC, f).offset, f
+
+
+def test_defaults_follow_reference_constructor():
+    p = CvoParams()
+    # CvoParams::CvoParams() (include/UnifiedCvo/cvo/CvoParams.hpp:80-136)
+    assert p.ell_init == pytest.approx(0.5)
+    assert p.sp_thres == pytest.approx(0.0006)
+    assert p.MAX_ITER == 10000
+    assert p.nearest_neighbors_max == 512
+    assert p.indicator_window_size == 15
+    assert p.is_using_geometry == 1 and p.is_using_intensity == 0
+    assert p.multiframe_iter_per_ell == 10
+
+
+def test_yaml_reader_sets_only_present_keys(tmp_path):
+    y = tmp_path / "p.yaml"
+    y.write_text("%YAML:1.0\n---\nell_init: 0.7 # comment\nMAX_ITER: 12\nis_ell_adaptive: False\n"
+                 "multiframe_iterations_per_ell: 33\nunknown_key: 5\n")
+    p = CvoParams(str(y))
+    assert p.ell_init == pytest.approx(0.7)
+    assert p.MAX_ITER == 12
+    assert p.sigma == pytest.approx(0.1)          # untouched default
+    assert p.multiframe_iterations_per_ell == 33  # the reference reads this key ...
+    assert p.multiframe_iter_per_ell == 10        # ... and never sets this field
+
+
+def test_yaml_reader_rejects_bad_values(tmp_path):
+    y = tmp_path / "bad.yaml"
+    y.write_text("MAX_ITER: 1.5\n")
+    with pytest.raises(L.CvoError) as e:
+        CvoParams(str(y))
+    assert e.value.code == L.CVO_ERR_BAD_YAML
+    with pytest.raises(L.CvoError) as e:
+        CvoParams(str(tmp_path / "missing.yaml"))
+    assert e.value.code == L.CVO_ERR_IO
+
+
+def test_bundled_param_files_parse():
+    for name in ("geometric", "color", "lidar_semantic", "irls"):
+        p = CvoParams(params_path(name))
+        assert p.MAX_ITER > 0
+    assert CvoParams(params_path("color")).nearest_neighbors_max == 256
+
+
+def test_status_strings():
+    lib = L.lib()
+    assert lib.cvo_status_string(0) == b"ok"
+    assert lib.cvo_status_string(L.CVO_ERR_BAD_YAML) == b"bad yaml parameter file"
+
+
+def test_handle_without_gpu_host_paths_work():
+    """Host entry points work on a handle; GPU entry points fail loudly when no GPU exists."""
+    cvo = CvoGPU(params=CvoParams())
+    a = CvoPointCloud(np.random.default_rng(0).uniform(0, 1, (50, 3)))
+    v = cvo.inner_product_cpu(a, a, np.eye(4), 0.1)
+    assert v > 0
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(L.CvoError) as e:
+            cvo.inner_product_gpu(a, a, np.eye(4), 0.1)
+        assert e.value.code == L.CVO_ERR_CUDA
+
+
+def test_empty_clouds_follow_reference_returns():
+    cvo = CvoGPU(params=CvoParams())
+    e = CvoPointCloud(np.zeros((0, 3)))
+    a = CvoPointCloud(np.ones((5, 3)))
+    # CvoGPU::align returns 0 on empty input, function_angle returns 0 (CvoGPU.cu:1492-1495,1773-1775)
+    ret, T, _, _, iters = cvo.align(e, a, np.eye(4))
+    assert ret == 0 and iters == 0
+    assert cvo.function_angle(e, a, np.eye(4), 0.1) == 0.0
+    assert cvo.inner_product_cpu(a, e, np.eye(4), 0.1) == 0.0
+    r = cvo.align_s2t(e, a, np.eye(4))
+    assert r.return_code == -1

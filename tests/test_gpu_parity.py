@@ -1,0 +1,198 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances (BASELINE the benchmark spec): neighbour sets bit-exact; inner products and
+kernel values within 1e-5 relative (the GPU evaluates kernel values with FP32
+exp and re-evaluates pairs near the threshold in FP64); final poses within
+1e-4 rad / 1e-4 m of the oracle's trajectory.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from rkhs_ba_gb300 import CvoGPU, CvoParams, CvoPointCloud, params_path, scenes
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def _rot_err(Ta, Tb):
+    R = Ta[:3, :3].astype(np.float64).T @ Tb[:3, :3].astype(np.float64)
+    s = 0.5 * np.linalg.norm([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]])
+    return float(np.arctan2(s, (np.trace(R) - 1) / 2))
+
+
+def _assoc_equal(a, ind, val, nnz):
+    """GPU CSR association vs oracle ELL: identical column sets per row, values within REL."""
+    n = a.rows
+    assert n == nnz.shape[0]
+    rp = a.row_ptr
+    assert int(rp[-1]) == int(nnz.sum())
+    for i in range(n):
+        cols = a.col[rp[i]:rp[i + 1]]
+        exp = ind[i, :nnz[i]]
+        assert np.array_equal(cols, exp), (i, cols[:8], exp[:8])
+        v = a.val[rp[i]:rp[i + 1]]
+        assert np.allclose(v, val[i, :nnz[i]], rtol=REL, atol=0), i
+
+
+def _pose(deg, axis, t):
+    return scenes.make_T(scenes.rot_axis_angle(axis, np.radians(deg)), t).astype(np.float32)
+
+
+@pytest.mark.parametrize("cap", [512, 24, 5])
+def test_association_room_bitexact(cuda_device, cap):
+    src, tgt, _ = scenes.room_pair(n=3000, seed=11)
+    p = CvoParams(params_path("geometric"))
+    p.nearest_neighbors_max = cap
+    cvo = CvoGPU(params=p)
+    T = _pose(3.0, [0.2, 1, 0.1], [0.05, -0.1, 0.02])
+    ell = 0.4
+    a = cvo.compute_association_gpu(src, tgt, T, ell)
+    ind, val, nnz = orc.association(p, src, tgt, T, ell, cap=cap)
+    _assoc_equal(a, ind, val, nnz)
+    if cap == 5:
+        assert (nnz == 5).sum() > 100      # the index-ordered truncation path ran
+    # inliers follow gpu_association_to_cpu: rows with pairs, one target entry per pair
+    assert np.array_equal(a.source_inliers, np.nonzero(nnz)[0])
+    assert a.target_inliers.shape[0] == a.nnz
+
+
+def test_association_color_bitexact(cuda_device):
+    src, tgt, _ = scenes.stereo_pair(n=4000, seed=2)
+    p = CvoParams(params_path("color"))
+    p.nearest_neighbors_max = 64
+    cvo = CvoGPU(params=p)
+    T = _pose(1.0, [0, 1, 0], [0, 0, 0.8])
+    a = cvo.compute_association_gpu(src, tgt, T, 0.5)
+    ind, val, nnz = orc.association(p, src, tgt, T, 0.5)
+    _assoc_equal(a, ind, val, nnz)
+    assert nnz.sum() > 1000
+
+
+def test_association_semantic_geotype_bitexact(cuda_device):
+    src, tgt, _ = scenes.lidar_pair(n=6000, seed=1)
+    rng = np.random.default_rng(0)
+    gs = rng.uniform(0.05, 1, size=(src.num_points(), 2)).astype(np.float32)
+    gt = rng.uniform(0.05, 1, size=(tgt.num_points(), 2)).astype(np.float32)
+    src = CvoPointCloud(src.xyz, src.features, src.labels, gs)
+    tgt = CvoPointCloud(tgt.xyz, tgt.features, tgt.labels, gt)
+    p = CvoParams(params_path("lidar_semantic"))
+    p.is_using_geometric_type = 1
+    p.nearest_neighbors_max = 32
+    cvo = CvoGPU(params=p)
+    a = cvo.compute_association_gpu(src, tgt, np.eye(4, dtype=np.float32), 0.6)
+    ind, val, nnz = orc.association(p, src, tgt, np.eye(4), 0.6)
+    _assoc_equal(a, ind, val, nnz)
+    assert nnz.sum() > 100
+
+
+@pytest.mark.parametrize("ell", [0.1, 0.3, 0.8])
+def test_inner_product_and_angle(cuda_device, ell):
+    src, tgt, _ = scenes.room_pair(n=4000, seed=5)
+    p = CvoParams(params_path("geometric"))
+    cvo = CvoGPU(params=p)
+    T = _pose(5.0, [1, 1, 0], [0.1, 0.2, -0.1])
+    g = cvo.inner_product_gpu(src, tgt, T, ell)
+    o, _ = orc.inner_product_gpu_semantics(p, src, tgt, T, ell)
+    assert g == pytest.approx(o, rel=REL)
+    ca = cvo.function_angle(src, tgt, T, ell, is_approximate=True)
+    assert ca == pytest.approx(orc.function_angle(p, src, tgt, T, ell, True, True), rel=REL)
+    ce = cvo.function_angle(src, tgt, T, ell, is_approximate=False)
+    assert ce == pytest.approx(orc.function_angle(p, src, tgt, T, ell, False, True), rel=REL)
+    # identical clouds at identity, exact mode: cos = 1
+    assert cvo.function_angle(src, src, np.eye(4), ell, is_approximate=False) == pytest.approx(1.0, rel=REL)
+
+
+def test_batched_inner_products_equal_single_calls(cuda_device):
+    src, tgt, _ = scenes.room_pair(n=3000, seed=6)
+    cvo = CvoGPU(params=CvoParams(params_path("geometric")))
+    gs, gt = cvo.upload(src), cvo.upload(tgt)
+    Ts = [_pose(d, [0, 0, 1], [0, 0, 0]) for d in (0, 10, 45, 90, 180)]
+    b = cvo.inner_product_batch(gs, gt, Ts, 0.3)
+    for k, T in enumerate(Ts):
+        assert b[k] == cvo.inner_product_gpu(gs, gt, T, 0.3)
+
+
+@pytest.mark.parametrize("max_iter", [1, 3, 40])
+def test_align_short_trajectory_matches_oracle(cuda_device, max_iter):
+    src, tgt, _ = scenes.room_pair(n=3000, seed=3)
+    p = CvoParams(params_path("geometric"))
+    p.MAX_ITER = max_iter
+    cvo = CvoGPU(params=p)
+    ret, T, _, _, iters = cvo.align(src, tgt, np.eye(4))
+    ret_o, T_o, iters_o, _ = orc.align(p, src, tgt, np.eye(4))
+    assert ret == ret_o and iters == iters_o
+    assert _rot_err(T, T_o) < 1e-4 and np.linalg.norm(T[:3, 3] - T_o[:3, 3]) < 1e-4
+
+
+def test_align_full_room_matches_oracle_and_truth(cuda_device):
+    src, tgt, T_gt = scenes.room_pair(n=3000, seed=3)
+    p = CvoParams(params_path("geometric"))
+    cvo = CvoGPU(params=p)
+    ret, T, _, secs, iters = cvo.align(src, tgt, np.eye(4))
+    ret_o, T_o, iters_o, _ = orc.align(p, src, tgt, np.eye(4))
+    assert ret == ret_o == 0
+    assert _rot_err(T, T_o) < 1e-4 and np.linalg.norm(T[:3, 3] - T_o[:3, 3]) < 1e-4
+    rot_deg, tr = scenes.pose_error(T, T_gt)
+    assert rot_deg < 1.0 and tr < 0.05
+
+
+def test_align_color_matches_oracle(cuda_device):
+    src, tgt, T_gt = scenes.stereo_pair(n=4000, seed=4)
+    p = CvoParams(params_path("color"))
+    p.MAX_ITER = 120
+    cvo = CvoGPU(params=p)
+    ret, T, _, _, iters = cvo.align(src, tgt, np.eye(4))
+    ret_o, T_o, iters_o, _ = orc.align(p, src, tgt, np.eye(4))
+    assert ret == ret_o and abs(iters - iters_o) <= 1
+    assert _rot_err(T, T_o) < 1e-4 and np.linalg.norm(T[:3, 3] - T_o[:3, 3]) < 1e-4
+
+
+def test_align_batch_equals_single(cuda_device):
+    p = CvoParams(params_path("geometric"))
+    p.MAX_ITER = 50
+    cvo = CvoGPU(params=p)
+    pairs = [scenes.room_pair(n=1500 + 500 * k, seed=20 + k) for k in range(3)]
+    gs = [cvo.upload(s) for s, _, _ in pairs]
+    gt = [cvo.upload(t) for _, t, _ in pairs]
+    Ts, rets, its, _ = cvo.align_batch(gs, gt, [np.eye(4)] * 3)
+    for k in range(3):
+        r1, T1, _, _, i1 = cvo.align(gs[k], gt[k], np.eye(4))
+        assert np.array_equal(T1, Ts[k]) and i1 == its[k] and r1 == rets[k]
+
+
+def test_nearest_init_pose_matches_oracle(cuda_device):
+    src, tgt, T_gt = scenes.room_pair(n=2000, seed=8, max_angle_deg=0.0, max_trans=0.0)
+    R = scenes.rot_axis_angle([0.3, -0.5, 0.8], np.radians(100))
+    tgt = CvoPointCloud((tgt.xyz.astype(np.float64) @ R.T).astype(np.float32))
+    p = CvoParams(params_path("geometric"))
+    cvo = CvoGPU(params=p)
+    for kind in (0, 1):
+        rots = CvoGPU.rotation_grid(kind)
+        T, _ = cvo.get_nearest_init_pose(src, tgt, 0.65, 0, kind)
+        bi, T_o, cos = orc.nearest_init_pose(p, src, tgt, 0.65, rots)
+        assert np.allclose(T, T_o)
+
+
+def test_align_s2t_and_association_export(cuda_device):
+    src, tgt, _ = scenes.room_pair(n=2000, seed=9)
+    p = CvoParams(params_path("geometric"))
+    p.MAX_ITER = 30
+    cvo = CvoGPU(params=p)
+    r = cvo.align_s2t(src, tgt, np.eye(4), is_returning_association=True)
+    assert r.return_code == 0 and r.num_iters == 30
+    assert r.association is not None and r.association.nnz > 0
+    # the exported association is the kernel matrix at the final pose and lengthscale
+    assert r.association.rows == src.num_points()
+
+
+def test_zero_gradient_return_code(cuda_device):
+    # clouds far apart: no pair within the kernel support -> zero gradient -> ret -1 at iteration 0
+    a = CvoPointCloud(np.random.default_rng(0).uniform(0, 1, (200, 3)))
+    b = CvoPointCloud(np.random.default_rng(1).uniform(0, 1, (200, 3)) + 100.0)
+    p = CvoParams(params_path("geometric"))
+    cvo = CvoGPU(params=p)
+    ret, T, _, _, iters = cvo.align(a, b, np.eye(4))
+    ret_o, T_o, iters_o, _ = orc.align(p, a, b, np.eye(4))
+    assert ret == ret_o == -1 and iters == iters_o == 0

@@ -1,0 +1,278 @@
+"""Pins the CPU oracle (oracle/cvo_oracle.c) with independent evidence:
+closed-form Lie-group identities, numpy restatements of the kernel matrix on
+tiny inputs, finite differences of the inner product, and the reference's own
+rotation grid and demo clouds where available."""
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from oracle import oracle as orc
+from rkhs_ba_gb300 import CvoGPU, CvoParams, CvoPointCloud, params_path, scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def hat(w):
+    return np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_exp_sek3_matches_matrix_exponential(seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=6).astype(np.float32)
+    v /= np.linalg.norm(v)
+    dt = float(rng.uniform(1e-4, 0.8))
+    X = orc.exp_sek3(v, dt)
+    tw = np.zeros((4, 4))
+    tw[:3, :3] = hat(v[:3].astype(np.float64)) * dt
+    tw[:3, 3] = v[3:].astype(np.float64) * dt
+    E = sla.expm(tw)
+    assert np.allclose(X, E[:3, :], atol=2e-6)
+
+
+def test_exp_sek3_small_rotation_branch():
+    # theta < 1e-6: R = I and Jl = I (LieGroup.cpp:253-256), so t = v regardless of dt
+    v = np.array([0, 0, 0, 0.3, -0.2, 0.1], np.float32)
+    X = orc.exp_sek3(v, 0.5)
+    assert np.allclose(X[:, :3], np.eye(3)) and np.allclose(X[:, 3], v[3:])
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_dist_se3_is_norm_of_log(seed):
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=3) * rng.uniform(0.01, 2.5) / 2
+    u = rng.normal(size=3)
+    tw = np.zeros((4, 4))
+    tw[:3, :3] = hat(w)
+    tw[:3, 3] = u
+    T = sla.expm(tw)
+    d = orc.dist_se3(T[:3, :3], T[:3, 3])
+    assert d == pytest.approx(np.sqrt(w @ w + u @ u), rel=1e-9, abs=1e-12)
+
+
+def test_cubic_roots_match_numpy():
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        c = rng.normal(size=4)
+        ok, re, im = orc.cubic_roots(*c)
+        assert ok
+        got = np.sort_complex(re + 1j * im)
+        want = np.sort_complex(np.roots(c))
+        assert np.allclose(got, want, atol=1e-7 * max(1, np.abs(want).max()))
+    ok, _, _ = orc.cubic_roots(0.0, 1.0, 2.0, 3.0)
+    assert not ok
+
+
+def test_step_rule():
+    p = CvoParams()
+    p.min_step, p.max_step = 1e-4, 0.8
+    # 4E s^3 + 3D s^2 + 2C s + B with roots 0.1, 0.3, -0.5 -> smallest positive = 0.1
+    poly = np.poly([0.1, 0.3, -0.5])
+    bcde = [poly[3], poly[2] / 2, poly[1] / 3, poly[0] / 4]
+    assert orc.step_from_terms(p, bcde) == pytest.approx(0.1, rel=1e-12)
+    # no positive real root -> temp stays max -> clamped to max_step
+    poly = np.poly([-0.1, -0.3, -0.5])
+    assert orc.step_from_terms(p, [poly[3], poly[2] / 2, poly[1] / 3, poly[0] / 4]) == pytest.approx(0.8, rel=1e-6)
+    # tiny root -> min_step
+    poly = np.poly([1e-7, 2.0, 3.0])
+    assert orc.step_from_terms(p, [poly[3], poly[2] / 2, poly[1] / 3, poly[0] / 4]) == pytest.approx(1e-4, rel=1e-6)
+    # degenerate (E == 0) -> max_step
+    assert orc.step_from_terms(p, [1.0, 1.0, 1.0, 0.0]) == pytest.approx(0.8, rel=1e-6)
+
+
+def _numpy_fill_A(p, src, ytr, cap, ell):
+    """Independent numpy restatement of fill_in_A_mat_gpu on tiny inputs (float32 ops in
+    the canonical order, kernel values with float64 exp)."""
+    f32 = np.float32
+    n, m = src.num_points(), ytr.shape[0]
+    sigma2 = f32(p.sigma) * f32(p.sigma)
+    logg = np.log(f32(p.sp_thres) / sigma2, dtype=np.float32)
+    out = []
+    for i in range(n):
+        x = src.xyz[i]
+        nrm = np.sqrt((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2], dtype=np.float32)
+        l = f32((float(nrm) / 500.0 + 1.0) * float(f32(ell)))
+        d2t = f32(-2.0 * float(l) * float(l) * float(logg))
+        row = []
+        for j in range(m):
+            if len(row) == cap:
+                break
+            y = ytr[j]
+            dx, dy, dz = y[0] - x[0], y[1] - x[1], y[2] - x[2]
+            d2 = (dx * dx + dy * dy) + dz * dz
+            if not d2 < d2t:
+                continue
+            k = f32(float(sigma2) * np.exp(-float(d2) / (2.0 * float(l) * float(l))))
+            a = f32(f32(f32(1.0) * k) * f32(1.0)) * f32(1.0)
+            if a > f32(p.sp_thres):
+                row.append((j, a))
+        out.append(row)
+    return out
+
+
+@pytest.mark.parametrize("cap", [512, 6])
+def test_oracle_kernel_matrix_matches_numpy_restatement(cap):
+    src, tgt, _ = scenes.room_pair(n=250, seed=4)
+    p = CvoParams(params_path("geometric"))
+    ell = 0.9
+    ytr = orc.transform_target(np.eye(4), tgt)
+    ind, val, nnz = orc.association(p, src, tgt, np.eye(4), ell, cap=cap)
+    ref = _numpy_fill_A(p, src, ytr, cap, ell)
+    total = 0
+    for i in range(src.num_points()):
+        assert nnz[i] == len(ref[i])
+        assert list(ind[i, :nnz[i]]) == [j for j, _ in ref[i]]
+        assert np.array_equal(val[i, :nnz[i]], np.array([a for _, a in ref[i]], np.float32))
+        total += nnz[i]
+    assert total > 0
+    if cap == 6:
+        assert (nnz == 6).sum() > 10   # truncation exercised
+
+
+def test_gradient_is_derivative_of_inner_product():
+    """d/ds <f(X), f(exp(-s xi) Y')> at s=0 equals sum_ij a_ij / l_i^2 (omega.(x x y) + v.(y - x))."""
+    src, tgt, _ = scenes.room_pair(n=400, seed=2)
+    p = CvoParams(params_path("geometric"))
+    p.sp_thres = 1e-9          # nearly every pair inside the kernel support: smooth objective
+    p.nearest_neighbors_max = 400
+    ell = 0.5
+    ytr = orc.transform_target(np.eye(4), tgt)
+    ind, val, nnz = orc.association(p, src, tgt, np.eye(4), ell)
+    g = orc.flow(p, src, ytr, ind, val, nnz)
+    w, v = g[:3] * p.c, g[3:] * p.d           # undo the 1/c, 1/d scaling
+    pred = 0.0
+    for i in range(src.num_points()):
+        x = src.xyz[i].astype(np.float64)
+        l = (np.linalg.norm(x) / 500.0 + 1.0) * ell
+        for t in range(nnz[i]):
+            y = ytr[ind[i, t]].astype(np.float64)
+            pred += val[i, t] / l ** 2 * (w @ np.cross(x, y) + v @ (y - x))
+
+    def F(s):
+        tw = np.zeros((4, 4))
+        tw[:3, :3] = hat(w)
+        tw[:3, 3] = v
+        T = sla.expm(s * tw)        # internal pose; the target moves by its inverse
+        return orc.inner_product_gpu_semantics(p, src, tgt, T, ell)[0]
+
+    h = 1e-3 / np.sqrt(w @ w + v @ v)
+    fd = (F(h) - F(-h)) / (2 * h)
+    assert fd == pytest.approx(pred, rel=2e-2)
+    assert pred > 0
+
+
+def test_step_terms_match_taylor_expansion():
+    """B is the first Taylor coefficient in s of sum_ij a_ij exp(-(|x - exp(-s xi) y|^2 - |x - y|^2)/(2l^2)).
+    (C, D, E follow the reference's own formulas, src/cvo/CvoGPU.cu:420-460, which are not
+    the exact higher-order coefficients; they are mirrored, not checked against the expansion.)"""
+    src, tgt, _ = scenes.room_pair(n=200, seed=5)
+    p = CvoParams(params_path("geometric"))
+    p.nearest_neighbors_max = 200
+    ell = 0.6
+    ytr = orc.transform_target(np.eye(4), tgt)
+    ind, val, nnz = orc.association(p, src, tgt, np.eye(4), ell)
+    g = orc.flow(p, src, ytr, ind, val, nnz)
+    xi = orc.normalize_grad(g).astype(np.float64)
+    bcde = orc.step_terms(p, src, ytr, ind, val, nnz, xi.astype(np.float32), ell)
+    W = hat(xi[:3])
+
+    def G(s):
+        tot = 0.0
+        for i in range(src.num_points()):
+            x = src.xyz[i].astype(np.float64)
+            for t in range(nnz[i]):
+                y = ytr[ind[i, t]].astype(np.float64)
+                # the target moves by exp(-s xi): z(s) = y - s u + s^2/2 W u - ..., u = W y + v
+                u = W @ y + xi[3:]
+                zs = y - s * u + s * s / 2 * (W @ u) - s ** 3 / 6 * (W @ W @ u) + s ** 4 / 24 * (W @ W @ W @ u)
+                d0 = x - y
+                ds = x - zs
+                tot += val[i, t] * np.exp(-(ds @ ds - d0 @ d0) / (2 * ell * ell))
+        return tot
+
+    ss = np.linspace(-0.02, 0.02, 9)
+    vals = np.array([G(s) for s in ss])
+    coef = np.polyfit(ss, vals, 4)[::-1]   # a0 + a1 s + ...
+    # sum a_ij exp(...) = sum a_ij (1 + B s + C s^2 + D s^3 + E s^4 + ...)
+    assert coef[1] == pytest.approx(bcde[0], rel=1e-3)
+
+
+def test_cpu_inner_product_library_matches_oracle():
+    src, tgt, _ = scenes.stereo_pair(n=2000, seed=1)
+    p = CvoParams(params_path("color"))
+    cvo = CvoGPU(params=p)
+    T = scenes.make_T(scenes.rot_axis_angle([0, 1, 0], 0.02), [0.1, 0, 0.3])
+    for ell in (0.3, 1.0):
+        lib_v = cvo.inner_product_cpu(src, tgt, T, ell)
+        orc_v, _ = orc.inner_product_cpu_semantics(p, src, tgt, T, ell)
+        assert lib_v == pytest.approx(orc_v, rel=1e-6)
+    # non-approximate CPU cos-angle of a cloud with itself is 1
+    assert cvo.function_angle(src, src, np.eye(4), 0.3, is_approximate=False, is_gpu=False) == pytest.approx(1.0, rel=1e-5)
+    assert orc.function_angle(p, src, src, np.eye(4), 0.3, False, False) == pytest.approx(1.0, rel=1e-5)
+
+
+def test_rotation_grids_are_groups():
+    for kind, n in ((0, 60), (1, 24)):
+        G = CvoGPU.rotation_grid(kind).astype(np.float64)
+        assert G.shape == (n, 3, 3)
+        for R in G:
+            assert np.allclose(R @ R.T, np.eye(3), atol=1e-6) and np.linalg.det(R) == pytest.approx(1, abs=1e-6)
+        # closed under composition
+        for a in range(0, n, 7):
+            for b in range(0, n, 5):
+                M = G[a] @ G[b]
+                assert np.min(np.abs(G - M).reshape(n, -1).max(1)) < 1e-5
+    assert CvoGPU.rotation_grid(2, 3).shape == (27, 3, 3)
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/src/cvo/CvoGPU.cpp"), reason="reference sources not mounted")
+def test_icosahedral_grid_equals_reference_set():
+    """The 60 rotations regenerated from the icosahedral symmetry are the set that
+    gen_icosahedron_init_rots (src/cvo/CvoGPU.cpp:279-342) lists (as a set, to float rounding)."""
+    import re
+    txt = open("/root/reference/src/cvo/CvoGPU.cpp").read()
+    ref = [np.array([float(v) for v in m.group(1).split(",")]).reshape(3, 3)
+           for m in re.finditer(r"pose\[\d+\]<<([^;]+);", txt)]
+    G = CvoGPU.rotation_grid(0).astype(np.float64)
+    assert len(ref) == 60
+    for R in ref:
+        assert np.min(np.abs(G - R).reshape(60, -1).max(1)) < 2e-6
+
+
+def test_demo_pcd_fixture_reads_like_reference():
+    """tests/golden/demo_pair.npz holds the demo clouds converted by tests/golden/make_golden.py;
+    reading them back through our PCD writer/reader round-trips exactly."""
+    d = np.load(os.path.join(GOLDEN, "demo_pair.npz"))
+    src = CvoPointCloud(d["src_xyz"], d["src_feat"], None, np.tile([[0, 1]], (d["src_xyz"].shape[0], 1)))
+    assert src.num_points() == 523 and d["tgt_xyz"].shape[0] == 1080
+    assert src.feature_dimensions() == 3
+    assert np.all((src.features >= 0) & (src.features <= 1))
+
+
+def test_pcd_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    f = (rng.integers(0, 256, size=(40, 3)) / 255.0).astype(np.float32)
+    c = CvoPointCloud(rng.normal(size=(40, 3)), f)
+    path = str(tmp_path / "a.pcd")
+    c.write_pcd(path)
+    r = CvoPointCloud.read_pcd(path)
+    assert np.array_equal(r.xyz, c.xyz)
+    assert np.allclose(r.features, c.features, atol=1e-7)
+    assert np.array_equal(r.geom_type, np.tile([[0, 1]], (40, 1)).astype(np.float32))
+
+
+def test_golden_oracle_outputs_stable():
+    """Regression pin of the oracle on the demo clouds (values generated by make_golden.py)."""
+    d = np.load(os.path.join(GOLDEN, "demo_pair.npz"))
+    g = np.load(os.path.join(GOLDEN, "demo_oracle.npz"))
+    src = CvoPointCloud(d["src_xyz"], d["src_feat"])
+    tgt = CvoPointCloud(d["tgt_xyz"], d["tgt_feat"])
+    p = CvoParams(params_path("color"))
+    p.MAX_ITER = int(g["max_iter"])
+    v, z = orc.inner_product_gpu_semantics(p, src, tgt, np.eye(4), float(g["ell"]))
+    assert z == int(g["ip_nnz"]) and v == pytest.approx(float(g["ip"]), rel=1e-12)
+    ret, T, iters, _ = orc.align(p, src, tgt, np.eye(4))
+    assert iters == int(g["iters"]) and np.allclose(T, g["T_out"], atol=1e-6)
