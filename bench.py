@@ -1,0 +1,340 @@
+"""Benchmark: global registration of 50k-point pairs on one GB300.
+
+Workload (one "step"): B seeded 50k-point pairs drawn like the colour/stereo
+configuration but with a uniformly random rotation and a shift <= 2 m; every pair
+is registered by the plain 24-rotation grid (cos-angle of each rotation at
+ell_init_first_frame, batched in one launch per pair), then all B pairs are refined
+together by the batched CVO align (one persistent batch, CUDA-graph chunks).
+The metric is registrations/s; success = rotation error < 2 deg and translation
+error < 5 cm against the generated ground truth.
+
+value : device-resident clouds (inputs already in HBM), whole-job registrations/s
+e2e   : the same through the C ABI from host buffers (cloud upload inside the timed region)
+roofline : the fused association kernel (k_assoc), algorithmic bytes / event-timed duration
+cpu_baseline : the CPU oracle (a restatement of the reference's CPU inner product and
+               align loop) on a bounded sample, scaled to registrations/s
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "registrations/s @50k pts: batched+learned vs plain grid, equal accuracy; HBM GB/s"
+UNIT = "registrations/s"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.th is not None:
+            self.th.join(timeout=2)
+        sm = []
+        reasons = set()
+        smax = None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax = float(r[1])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if r[4 + k].lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_pairs(n_pairs, n_points, seed0=1000):
+    from rkhs_ba_gb300 import scenes
+    return [scenes.global_pair(n=n_points, seed=seed0 + k) for k in range(n_pairs)]
+
+
+def run_ours(args):
+    import torch
+    from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    p = CvoParams(params_path("color"))
+    if args.max_iter > 0:
+        p.MAX_ITER = args.max_iter
+    cvo = CvoGPU(params=p)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    cvo.set_stream(stream.cuda_stream)
+    pairs = make_pairs(args.pairs, args.points, seed0=1000 + 100 * rank)
+    grid = CvoGPU.rotation_grid(1)  # 24-rotation grid
+
+    def register(gs, gt):
+        inits = []
+        for s, t in zip(gs, gt):
+            T, _ = cvo.get_nearest_init_pose(s, t, p.ell_init_first_frame, 0, 1)
+            inits.append(scenes.inv_T(T))        # CvoGPU::align(int overload) inverts the grid pose
+        Ts, rets, its, _ = cvo.align_batch(gs, gt, inits)
+        return Ts, its
+
+    gs = [cvo.upload(s) for s, _, _ in pairs]
+    gt = [cvo.upload(t) for _, t, _ in pairs]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
+
+    for _ in range(args.warmup):
+        register(gs, gt)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    # ---- device-resident timed region
+    cvo.profile(True)
+    cvo.profile_reset()
+    launches0 = cvo.kernel_launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = []
+    results = []
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        Ts, its = register(gs, gt)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        results.append((Ts, its))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    launches = cvo.kernel_launches - launches0
+    prof = cvo.profile_read()
+    cvo.profile(False)
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_reg = args.pairs * args.steps * world
+    value = n_reg / (total_ms / 1000.0)
+
+    # accuracy of the last step
+    succ = []
+    iters = []
+    for (Ts, its) in results[-1:]:
+        for k, (_, _, T_gt) in enumerate(pairs):
+            r, tr = scenes.pose_error(Ts[k], T_gt)
+            succ.append(r < 2.0 and tr < 0.05)
+            iters.append(int(its[k]))
+
+    # ---- end-to-end through the C ABI from host buffers
+    h2d = sum(s.xyz.nbytes + s.features.nbytes + t.xyz.nbytes + t.features.nbytes for s, t, _ in pairs)
+    d2h = args.pairs * (16 * 4 + 24 * 4)
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for k in range(max(1, min(args.steps, 2))):
+        flush.fill_(float(k))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        hs = [cvo.upload(s) for s, _, _ in pairs]
+        ht = [cvo.upload(t) for _, t, _ in pairs]
+        register(hs, ht)
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+        for c in hs + ht:
+            c.free()
+    e2e_value = args.pairs / (float(np.mean(e2e_ms)) / 1000.0) * world
+
+    # ---- roofline of the association kernel
+    peak, peak_kind = _peaks()
+    roof = None
+    if prof["assoc_launches"] > 0 and prof["assoc_ms"] > 0:
+        per_launch_bytes = prof["assoc_bytes"] / prof["assoc_launches"]
+        avg_s = prof["assoc_ms"] / prof["assoc_launches"] / 1000.0
+        achieved = per_launch_bytes / avg_s / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "assoc_traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as fh:
+                traffic = json.load(fh).get("dram_bytes_per_launch")
+        roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "k_assoc", "launches": prof["assoc_launches"],
+                "avg_launch_us": round(avg_s * 1e6, 3), "algorithmic_bytes_per_launch": round(per_launch_bytes),
+                "iteration_kernel_ms": {k: round(v, 3) for k, v in prof["kernel_ms"].items()}}
+
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+        "config": {"workload": "global registration, plain 24-rotation grid + batched CVO refine",
+                   "points_per_cloud": args.points, "pairs_per_step": args.pairs, "params": "color.yaml",
+                   "rotation": "uniform SO(3)", "translation_max_m": 2.0,
+                   "l2": "256 MB buffer written between timed steps", "parallelism": "replicas"},
+        "accuracy": {"success_rate": float(np.mean(succ)) if succ else None, "criterion": "rot<2deg, trans<5cm",
+                     "mean_iters": float(np.mean(iters)) if iters else None},
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk,
+        "wall_s": round(wall, 3),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, pairs[0], float(np.mean(iters)) if iters else 100.0)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, pair, iters_per_reg, budget_s=None):
+    """The CPU oracle on a bounded sample of the workload: the 24-rotation grid with the
+    reference's CPU inner product (radius search, all host threads) on one pair, plus a
+    few iterations of the CPU align loop; scaled to one registration using the GPU
+    run's mean iteration count."""
+    from oracle import oracle as orc
+    from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path
+
+    p = CvoParams(params_path("color"))
+    src, tgt, _ = pair
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    grid = CvoGPU.rotation_grid(1)
+    n_rot = len(grid) if args.cpu_rotations <= 0 else min(args.cpu_rotations, len(grid))
+    t0 = time.perf_counter()
+    for r in range(n_rot):
+        T = np.eye(4, dtype=np.float32)
+        T[:3, :3] = grid[r].T
+        orc.function_angle(p, src, tgt, T, p.ell_init_first_frame, True, False)
+    t_grid = (time.perf_counter() - t0) * len(grid) / n_rot
+    q = p.copy()
+    q.MAX_ITER = args.cpu_iters
+    t0 = time.perf_counter()
+    orc.align(q, src, tgt, np.eye(4))
+    t_iter = (time.perf_counter() - t0) / args.cpu_iters
+    per_reg = t_grid + t_iter * iters_per_reg
+    return {"value": round(1.0 / per_reg, 6), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of 24 grid cos-angles (reference CPU inner-product semantics) + %d align iterations "
+                      "on one %d-point pair; scaled to 24 rotations + %.0f iterations per registration"
+                      % (n_rot, args.cpu_iters, src.num_points(), iters_per_reg),
+            "seconds_per_registration": round(per_reg, 3)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pairs = make_pairs(1, args.points)
+    samples = []
+    t_all = time.perf_counter()
+    cb = None
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(args, pairs[0], args.ref_iters)
+        samples.append(1.0 / cb["seconds_per_registration"])
+    value = float(np.mean(samples))
+    out = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "impl": "reference", "n_gpus": 1,
+           "steps": args.steps, "warmup": 0, "ms_per_step": round(1000.0 / value, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+           "config": {"workload": "global registration, plain 24-rotation grid + CVO refine (CPU)",
+                      "points_per_cloud": args.points, "pairs_per_step": 1, "params": "color.yaml",
+                      "note": "reference CPU path restated (the reference cannot be compiled here)"},
+           "cpu_baseline": {"kind": "port", "cores": cb["cores"], "sample": cb["sample"], "value": round(value, 6),
+                            "unit": UNIT},
+           "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "wall_s": round(time.perf_counter() - t_all, 3)}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs", type=int, default=8)
+    ap.add_argument("--points", type=int, default=50000)
+    ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--cpu-rotations", type=int, default=4)
+    ap.add_argument("--ref-iters", type=float, default=100.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
+    args = ap.parse_args()
+    from rkhs_ba_gb300 import _build
+    _build.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

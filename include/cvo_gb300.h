@@ -265,6 +265,24 @@ const char *cvo_status_string(int status);
 /* Number of kernel launches this handle has issued since creation (all kernels
  * of this library; used by benchmarks to report launch counts). */
 int64_t cvo_kernel_launch_count(const cvo_handle *h);
+/* Stream used by the handle's work (a cudaStream_t passed as void*).  The
+ * reference runs everything on the default stream; here a caller may hand its
+ * own stream so that its CUDA events bracket the library's kernels.  NULL
+ * restores the handle's private stream. */
+int cvo_set_stream(cvo_handle *h, void *cuda_stream);
+void *cvo_get_stream(const cvo_handle *h);
+/* Kernel profiling (no reference counterpart; the reference only times the
+ * whole align loop with cudaEvents, src/cvo/CvoGPU.cu:1270-1273,1436-1465).
+ * When enabled, every association-kernel launch of the align loop is bracketed
+ * by CUDA events on the handle's stream and its algorithmic bytes
+ * ((N + M) * record_bytes + 4 N + 8 nnz per pair) are accumulated. */
+int cvo_profile_enable(cvo_handle *h, int on);
+int cvo_profile_read(const cvo_handle *h, double *assoc_ms, int64_t *assoc_launches,
+                     double *assoc_bytes, int64_t *iterations);
+int cvo_profile_reset(cvo_handle *h);
+/* Accumulated event-timed milliseconds of the kernels of the align iterations:
+ * [transform, association, reduction, step, all four]. */
+int cvo_profile_kernels(const cvo_handle *h, double ms[5]);
 /* Last CUDA error text recorded by the handle (empty if none). */
 const char *cvo_last_error(const cvo_handle *h);
 

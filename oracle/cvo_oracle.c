@@ -165,7 +165,8 @@ static int cmp_kj(const void *a, const void *b) {
   if (x->key != y->key) return x->key < y->key ? -1 : 1;
   return x->j - y->j;
 }
-static int cmp_int(const void *a, const void *b) { int x = *(const int *)a, y = *(const int *)b; return (x > y) - (x < y); }
+typedef struct { int j; float a; } ja_t;
+static int cmp_ja(const void *a, const void *b) { int x = ((const ja_t *)a)->j, y = ((const ja_t *)b)->j; return (x > y) - (x < y); }
 
 static int64_t cell_key(int64_t cx, int64_t cy, int64_t cz) {
   return ((cx + (1 << 20)) << 42) | ((cy + (1 << 20)) << 21) | (cz + (1 << 20));
@@ -194,7 +195,7 @@ static void grid_build(grid_t *g, const float *pts, int n, float h) {
 }
 static void grid_free(grid_t *g) { free(g->ent); g->ent = NULL; }
 
-/* Collect every target within the 27 neighbour cells of x, ascending index. */
+/* Collect every target within the 27 neighbour cells of x (in cell order). */
 static int grid_candidates(const grid_t *g, const float *x, int *buf, int cap_buf) {
   if (g->brute) { for (int j = 0; j < g->n && j < cap_buf; j++) buf[j] = j; return g->n; }
   int64_t cx = (int64_t)floor((x[0] - g->ox) / g->h);
@@ -209,7 +210,6 @@ static int grid_candidates(const grid_t *g, const float *x, int *buf, int cap_bu
         while (lo < hi) { int mid = (lo + hi) / 2; if (g->ent[mid].key < key) lo = mid + 1; else hi = mid; }
         for (int t = lo; t < g->n && g->ent[t].key == key; t++) { if (cnt < cap_buf) buf[cnt] = g->ent[t].j; cnt++; }
       }
-  if (cnt <= cap_buf) qsort(buf, (size_t)cnt, sizeof(int), cmp_int);
   return cnt;
 }
 
@@ -238,6 +238,7 @@ int orc_fill_A(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, 
   {
     int bufcap = m > 0 ? m : 1;
     int *buf = (int *)malloc(sizeof(int) * (size_t)bufcap);
+    ja_t *kept = (ja_t *)malloc(sizeof(ja_t) * (size_t)bufcap);
 #pragma omp for schedule(dynamic, 64)
     for (int i = 0; i < n; i++) {
       float x[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
@@ -246,23 +247,32 @@ int orc_fill_A(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, 
       if (k.use_geo) d2t = geo_d2_thres(&k, l);
       int nc = grid_candidates(&g, x, buf, bufcap);
       if (nc > bufcap) { fail = 1; nc = bufcap; }
-      int cnt = 0;
-      for (int t = 0; t < nc && cnt < cap; t++) {
+      /* every kept pair of the row, then the first `cap` of them in ascending
+       * target index: the set the reference's index-ordered scan keeps */
+      int nk = 0;
+      for (int t = 0; t < nc; t++) {
         int j = buf[t];
         float a;
         if (pair_value_gpu(&k, p, x, F ? src->features + (size_t)i * F : NULL, C ? src->labels + (size_t)i * C : NULL,
                            src->geom_type ? src->geom_type + 2 * (size_t)i : NULL, ytr + 3 * (size_t)j,
                            F ? tgt->features + (size_t)j * F : NULL, C ? tgt->labels + (size_t)j * C : NULL,
                            tgt->geom_type ? tgt->geom_type + 2 * (size_t)j : NULL, F, C, l, d2t, &a)) {
-          ind[(size_t)i * cap + cnt] = j;
-          val[(size_t)i * cap + cnt] = a;
-          cnt++;
+          kept[nk].j = j;
+          kept[nk].a = a;
+          nk++;
         }
+      }
+      qsort(kept, (size_t)nk, sizeof(ja_t), cmp_ja);
+      int cnt = nk < cap ? nk : cap;
+      for (int t = 0; t < cnt; t++) {
+        ind[(size_t)i * cap + t] = kept[t].j;
+        val[(size_t)i * cap + t] = kept[t].a;
       }
       for (int t = cnt; t < cap; t++) { ind[(size_t)i * cap + t] = -1; val[(size_t)i * cap + t] = 0.f; }
       nnz[i] = cnt;
     }
     free(buf);
+    free(kept);
   }
   grid_free(&g);
   return fail ? -1 : 0;

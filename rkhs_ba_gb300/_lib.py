@@ -99,6 +99,12 @@ SIGNATURES = {
     "cvo_status_string": (C.c_char_p, [_i]),
     "cvo_kernel_launch_count": (C.c_int64, [_P]),
     "cvo_last_error": (C.c_char_p, [_P]),
+    "cvo_set_stream": (_i, [_P, _P]),
+    "cvo_get_stream": (_P, [_P]),
+    "cvo_profile_enable": (_i, [_P, _i]),
+    "cvo_profile_read": (_i, [_P, _DP, C.POINTER(C.c_int64), _DP, C.POINTER(C.c_int64)]),
+    "cvo_profile_reset": (_i, [_P]),
+    "cvo_profile_kernels": (_i, [_P, _DP]),
 }
 
 _LIB = None

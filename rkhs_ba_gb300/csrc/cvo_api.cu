@@ -227,8 +227,9 @@ static int init_handle(cvo_handle *H) {
   if (e != cudaSuccess) return set_cuda_error(&h, e, "cudaGetDevice");
   e = cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, h.device);
   if (e != cudaSuccess) return set_cuda_error(&h, e, "cudaDeviceGetAttribute");
-  e = cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking);
+  e = cudaStreamCreateWithFlags(&h.own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return set_cuda_error(&h, e, "cudaStreamCreate");
+  h.stream = h.own_stream;
   return CVO_OK;
 }
 
@@ -256,7 +257,7 @@ extern "C" int cvo_destroy(cvo_handle *H) {
   if (!H) return CVO_ERR_INVALID_ARG;
   if (H->h.stream) cudaStreamSynchronize(H->h.stream);
   free_workspace(&H->h);
-  if (H->h.stream) cudaStreamDestroy(H->h.stream);
+  if (H->h.own_stream) cudaStreamDestroy(H->h.own_stream);
   delete H;
   return CVO_OK;
 }
@@ -292,6 +293,46 @@ extern "C" const char *cvo_status_string(int s) {
 
 extern "C" int64_t cvo_kernel_launch_count(const cvo_handle *H) { return H ? H->h.launches : 0; }
 extern "C" const char *cvo_last_error(const cvo_handle *H) { return H ? H->h.last_error.c_str() : ""; }
+
+extern "C" int cvo_set_stream(cvo_handle *H, void *stream) {
+  if (!H) return CVO_ERR_INVALID_ARG;
+  if (!H->h.own_stream) return CVO_ERR_CUDA;
+  cudaStreamSynchronize(H->h.stream);
+  H->h.stream = stream ? (cudaStream_t)stream : H->h.own_stream;
+  return CVO_OK;
+}
+
+extern "C" void *cvo_get_stream(const cvo_handle *H) { return H ? (void *)H->h.stream : nullptr; }
+
+extern "C" int cvo_profile_enable(cvo_handle *H, int on) {
+  if (!H) return CVO_ERR_INVALID_ARG;
+  H->h.prof.on = on != 0;
+  return CVO_OK;
+}
+
+extern "C" int cvo_profile_read(const cvo_handle *H, double *assoc_ms, int64_t *assoc_launches, double *assoc_bytes,
+                                int64_t *iterations) {
+  if (!H) return CVO_ERR_INVALID_ARG;
+  if (assoc_ms) *assoc_ms = H->h.prof.assoc_ms;
+  if (assoc_launches) *assoc_launches = H->h.prof.assoc_launches;
+  if (assoc_bytes) *assoc_bytes = H->h.prof.assoc_bytes;
+  if (iterations) *iterations = H->h.prof.iterations;
+  return CVO_OK;
+}
+
+extern "C" int cvo_profile_kernels(const cvo_handle *H, double ms[5]) {
+  if (!H || !ms) return CVO_ERR_INVALID_ARG;
+  for (int k = 0; k < 5; k++) ms[k] = H->h.prof.kernel_ms[k];
+  return CVO_OK;
+}
+
+extern "C" int cvo_profile_reset(cvo_handle *H) {
+  if (!H) return CVO_ERR_INVALID_ARG;
+  bool on = H->h.prof.on;
+  H->h.prof = Profile();
+  H->h.prof.on = on;
+  return CVO_OK;
+}
 
 // ----------------------------------------------------------------- clouds
 extern "C" int cvo_cloud_upload(cvo_handle *H, const cvo_cloud *c, cvo_gpu_cloud **out) {

@@ -74,6 +74,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(BatchDev B, KParams K
     tot[8] = fmax(tot[8], pv[(size_t)bb * kPartStride + 8]);
   }
   P->counter[0] = 0;
+  // algorithmic bytes of this pair's association pass: every source and target
+  // record once, the per-row count, and the ELL entries when they are written
+  atomicAdd(B.assoc_bytes, (double)(P->n + P->m) * B.record_bytes + 4.0 * P->n +
+                               (P->mode != MODE_IP ? 8.0 * tot[7] : 0.0));
   for (int k = 0; k < 6; k++) P->grad[k] = tot[k];
   P->asum = tot[6];
   P->nnz_sum = (long long)tot[7];
@@ -228,11 +232,11 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
     float tl = K.use_range_ell_step ? range_ell(P->ell, x.w) : P->ell;
     float coef = __double2float_rn(__ddiv_rn(1.0, dm(dm(2.0, (double)tl), (double)tl)));
     const int z = P->nnz_row[s];
-    const float4 *__restrict__ ycur = P->ycur;
+    const float4 *__restrict__ yorig = P->yorig;
     for (int c = 0; c < z; c++) {
-      int t = P->A_j[(size_t)c * n + s];
+      int j = P->A_j[(size_t)c * n + s];
       float a = P->A_v[(size_t)c * n + s];
-      float4 y = __ldg(&ycur[t]);
+      float4 y = __ldg(&yorig[j]);
       float ux = w1 * y.z - w2 * y.y + u0v, uy = w2 * y.x - w0 * y.z + u1v, uz = w0 * y.y - w1 * y.x + u2v;
       float px = w1 * uz - w2 * uy, py = w2 * ux - w0 * uz, pz = w0 * uy - w1 * ux;          // xi^2 z
       float qx = w1 * pz - w2 * py, qy = w2 * px - w0 * pz, qz = w0 * py - w1 * px;          // xi^3 z
@@ -283,38 +287,32 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
 // ----------------------------------------------------- association export
 // Rows of the last association as (original row, original column, value),
 // written into a compact buffer at row offsets computed on the host.
-__global__ void k_export(const PairDev *P, const int *row_start, int *cols, float *vals, const int *tperm) {
+__global__ void k_export(const PairDev *P, const int *row_start, int *cols, float *vals) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= P->n) return;
   int z = P->nnz_row[s];
   int o = row_start[s];
   for (int c = 0; c < z; c++) {
-    cols[o + c] = tperm[P->A_j[(size_t)c * P->n + s]];
+    cols[o + c] = P->A_j[(size_t)c * P->n + s];
     vals[o + c] = P->A_v[(size_t)c * P->n + s];
   }
 }
 
 // --------------------------------------------------------- template dispatch
 using AssocFn = void (*)(BatchDev, KParams);
-using OvfFn = void (*)(BatchDev, KParams);
 
-template <int FCH, int LCH, bool GT>
-void pick(AssocFn &a, OvfFn &o) {
-  a = k_assoc<FCH, LCH, GT>;
-  o = k_overflow<FCH, LCH, GT>;
-}
-
-int select_kernels(const KParams &K, int F, int C, AssocFn &a, OvfFn &o) {
+// Feature rows are stored as ceil(F/4) float4 chunks; label rows as 5 or 9
+// chunks (C <= 20 or C <= 36, padded at upload), so the chunk counts below are
+// the storage strides of the clouds.
+int select_kernels(const KParams &K, int F, int C, AssocFn &a) {
   int fch = K.use_int ? (F + 3) / 4 : 0;
-  int lch = K.use_sem ? (C + 3) / 4 : 0;
+  int lch = K.use_sem ? label_chunks(C) : 0;
   bool gt = K.use_gtype != 0;
   if (fch > 2 || lch > 9) return CVO_ERR_UNSUPPORTED;
-  if (lch > 0 && lch <= 5) lch = 5;
-  else if (lch > 5) lch = 9;
 #define CVO_PICK(FC, LC)                         \
   if (fch == FC && lch == LC) {                  \
-    if (gt) pick<FC, LC, true>(a, o);            \
-    else pick<FC, LC, false>(a, o);              \
+    if (gt) a = k_assoc<FC, LC, true>;           \
+    else a = k_assoc<FC, LC, false>;             \
     return 0;                                    \
   }
   CVO_PICK(0, 0) CVO_PICK(1, 0) CVO_PICK(2, 0)
@@ -419,8 +417,7 @@ struct BatchHost {
   std::vector<int> tile_off, row_off, tgt_off, rblk_off, sblk_off;
   float *src_max_norm = nullptr;
   AssocFn assoc = nullptr;
-  OvfFn ovf = nullptr;
-  int assoc_blocks = 0, ovf_blocks = 0, xform_blocks = 0;
+  int assoc_blocks = 0, xform_blocks = 0;
 };
 
 // Lays out every device buffer of a batch in the handle's workspace.
@@ -433,7 +430,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     if (srcs[p]->F != F || tgts[p]->F != F || srcs[p]->C != C || tgts[p]->C != C) return CVO_ERR_INVALID_ARG;
     if (K.use_gtype && (!srcs[p]->has_geo || !tgts[p]->has_geo)) return CVO_ERR_INVALID_ARG;
   }
-  int rc = select_kernels(K, F, C, bh->assoc, bh->ovf);
+  int rc = select_kernels(K, F, C, bh->assoc);
   if (rc) return rc;
   // grid levels per pair
   std::vector<std::vector<GridDesc>> lv(np);
@@ -479,7 +476,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     bh->sblk_off[p + 1] = bh->sblk_off[p] + sb;
     max_part_blocks = std::max(max_part_blocks, std::max(rb, sb));
     add(sizeof(float4) * m);                                     // ycur
-    if (mode != MODE_IP) { add(sizeof(int) * (size_t)n * capmax); add(sizeof(float) * (size_t)n * capmax); }
+    add(sizeof(float4) * m);                                     // yorig
+    add(sizeof(int) * (size_t)n * capmax);                       // ELL (every mode: the row selection uses it)
+    add(sizeof(float) * (size_t)n * capmax);
     add(sizeof(int) * n);                                        // nnz_row
     add(sizeof(float) * 8 * (size_t)n);                          // row_sums
     add(sizeof(double) * kPartStride * (size_t)std::max(rb, sb)); // partials
@@ -489,7 +488,6 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   const int total_rows = bh->row_off[np];
   add(sizeof(PairDev) * np);
   add(sizeof(int) * (np + 1) * 5);
-  add(sizeof(OvfEntry) * std::max(total_rows, 1));
   add(sizeof(int) * 4);
   add(sizeof(float) * np);
   if ((rc = ensure_workspace(h, bytes))) return rc;
@@ -506,7 +504,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     P.n = s->n; P.m = t->n; P.F = F; P.C = C;
     P.xs = s->spos; P.xf = s->sfeat; P.xl = s->slab; P.xg = s->sgeo; P.sperm = s->sperm;
     P.ycur = ar.take<float4>(t->n);
-    if (mode != MODE_IP) { P.A_j = ar.take<int>((size_t)s->n * capmax); P.A_v = ar.take<float>((size_t)s->n * capmax); }
+    P.yorig = ar.take<float4>(t->n);
+    P.A_j = ar.take<int>((size_t)s->n * capmax);
+    P.A_v = ar.take<float>((size_t)s->n * capmax);
     P.nnz_row = ar.take<int>(s->n);
     P.row_sums = ar.take<float>(8 * (size_t)s->n);
     int rb = bh->rblk_off[p + 1] - bh->rblk_off[p], sb = bh->sblk_off[p + 1] - bh->sblk_off[p];
@@ -543,8 +543,8 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   }
   PairDev *pairs_d = ar.take<PairDev>(np);
   int *offs_d = ar.take<int>((size_t)(np + 1) * 5);
-  OvfEntry *ovf_d = ar.take<OvfEntry>(std::max(total_rows, 1));
   int *ctr_d = ar.take<int>(4);
+  double *bytes_d = ar.take<double>(1);
   bh->src_max_norm = ar.take<float>(np);
   // zero counters of every pair
   for (int p = 0; p < np; p++) CVO_CUDA_TRY(h, cudaMemsetAsync(bh->pairs[p].counter, 0, 2 * sizeof(unsigned), h->stream));
@@ -559,6 +559,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   CVO_CUDA_TRY(h, cudaMemcpyAsync(bh->src_max_norm, mn.data(), sizeof(float) * np, cudaMemcpyHostToDevice, h->stream));
   int ctr_h[4] = {0, 0, active, 0};
   CVO_CUDA_TRY(h, cudaMemcpyAsync(ctr_d, ctr_h, sizeof(ctr_h), cudaMemcpyHostToDevice, h->stream));
+  CVO_CUDA_TRY(h, cudaMemsetAsync(bytes_d, 0, sizeof(double), h->stream));
   CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   BatchDev &B = bh->B;
   memset(&B, 0, sizeof(B));
@@ -574,29 +575,42 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   B.sblk_off = offs_d + 4 * (np + 1);
   B.total_rblocks = bh->rblk_off[np];
   B.total_sblocks = bh->sblk_off[np];
-  B.ovf = ovf_d;
-  B.ovf_n = ctr_d;
-  B.ovf_cap = std::max(total_rows, 1);
   B.err = ctr_d + 1;
   B.active = ctr_d + 2;
+  B.active_iters = ctr_d + 3;
+  B.assoc_bytes = bytes_d;
+  {
+    int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
+    B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
+  }
   bh->assoc_blocks = (B.total_warps * 32 + kAssocThreads - 1) / kAssocThreads;
   bh->xform_blocks = (B.total_targets + 255) / 256;
-  bh->ovf_blocks = std::max(1, h->num_sms * 4);
   return 0;
 }
 
-void launch_association(Handle *h, BatchHost *bh, const KParams &K) {
-  BatchDev &B = bh->B;
-  k_transform<<<std::max(bh->xform_blocks, 1), 256, 0, h->stream>>>(B);
-  bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, 0, h->stream>>>(B, K);
-  bh->ovf<<<bh->ovf_blocks, kOvfThreads, 0, h->stream>>>(B, K);
-  k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
-  h->launches += 4;
+// Inside stream capture an event becomes a record node of the graph only with
+// cudaEventRecordExternal (a plain cudaEventRecord only adds a dependency).
+inline void mark(Handle *h, const cudaEvent_t *ev, int k) {
+  if (ev) cudaEventRecordWithFlags(ev[k], h->stream, cudaEventRecordExternal);
 }
 
-void launch_iteration(Handle *h, BatchHost *bh, const KParams &K) {
-  launch_association(h, bh, K);
+// ev (optional): 5 events bracketing transform, assoc, reduce, step.
+void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEvent_t *ev = nullptr) {
+  BatchDev &B = bh->B;
+  mark(h, ev, 0);
+  k_transform<<<std::max(bh->xform_blocks, 1), 256, 0, h->stream>>>(B);
+  mark(h, ev, 1);
+  bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, 0, h->stream>>>(B, K);
+  mark(h, ev, 2);
+  k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
+  mark(h, ev, 3);
+  h->launches += 3;
+}
+
+void launch_iteration(Handle *h, BatchHost *bh, const KParams &K, const cudaEvent_t *ev = nullptr) {
+  launch_association(h, bh, K, ev);
   k_step<<<std::max(bh->B.total_sblocks, 1), kStepThreads, 0, h->stream>>>(bh->B, K, bh->src_max_norm);
+  mark(h, ev, 4);
   h->launches += 1;
 }
 
@@ -634,16 +648,9 @@ int export_pair(Handle *h, BatchHost *bh, int p, DevCloud *src, DevCloud *tgt, s
   CVO_CUDA_TRY(h, cudaMalloc((void **)&cols_d, sizeof(int) * std::max(total, 1)));
   CVO_CUDA_TRY(h, cudaMalloc((void **)&vals_d, sizeof(float) * std::max(total, 1)));
   CVO_CUDA_TRY(h, cudaMemcpyAsync(start_d, start.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
-  GridDesc g = tgt->levels_host.begin()->second;
-  {
-    // level used by the last association of this pair
-    std::vector<GridDesc> lv(P.nlevels);
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(lv.data(), P.levels, sizeof(GridDesc) * P.nlevels, cudaMemcpyDeviceToHost, h->stream));
-    CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    g = lv[P.level_used];
-  }
+  (void)tgt;
   PairDev *pd = bh->B.pairs + p;
-  k_export<<<(n + 255) / 256, 256, 0, h->stream>>>(pd, start_d, cols_d, vals_d, g.perm);
+  k_export<<<(n + 255) / 256, 256, 0, h->stream>>>(pd, start_d, cols_d, vals_d);
   h->launches++;
   std::vector<int> c(total);
   std::vector<float> v(total);
@@ -694,20 +701,54 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   long long before = h->launches;
+  // with profiling on, every kernel launch of the chunk is bracketed by
+  // event-record nodes of the graph
+  constexpr int kEv = 5;
+  std::vector<cudaEvent_t> pev;
+  if (h->prof.on) {
+    pev.resize(kEv * kChunk);
+    for (auto &e : pev) cudaEventCreate(&e);
+  }
   CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int it = 0; it < kChunk; it++) launch_iteration(h, &bh, K);
+  for (int it = 0; it < kChunk; it++) launch_iteration(h, &bh, K, h->prof.on ? &pev[kEv * it] : nullptr);
   CVO_CUDA_TRY(h, cudaStreamEndCapture(h->stream, &graph));
   long long per_chunk = h->launches - before;
   h->launches = before;
   CVO_CUDA_TRY(h, cudaGraphInstantiate(&exec, graph, 0));
   int *active_h = h->ws->pinned;
   long long max_chunks = (long long)h->params.MAX_ITER / kChunk + 2;
+  long long iters_seen = 0;
   for (long long ch = 0; ch < max_chunks; ch++) {
     CVO_CUDA_TRY(h, cudaGraphLaunch(exec, h->stream));
     h->launches += per_chunk;
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(active_h, bh.B.active, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(active_h, bh.B.active, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (h->prof.on) {
+      // active_h[1]: iterations (so far) that started with at least one active pair
+      long long act = active_h[1];
+      for (int it = 0; it < kChunk; it++) {
+        if (ch * kChunk + it >= act) break;
+        for (int k = 0; k < 4; k++) {
+          float ms = 0.f;
+          if (cudaEventElapsedTime(&ms, pev[kEv * it + k], pev[kEv * it + k + 1]) == cudaSuccess) {
+            h->prof.kernel_ms[k] += ms;
+            h->prof.kernel_ms[4] += ms;
+          }
+        }
+        h->prof.assoc_launches++;
+      }
+      iters_seen = act;
+    }
     if (*active_h <= 0) break;
+  }
+  if (h->prof.on) {
+    double bytes = 0;
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(&bytes, bh.B.assoc_bytes, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->prof.assoc_bytes += bytes;
+    h->prof.iterations += iters_seen;
+    h->prof.assoc_ms = h->prof.kernel_ms[1];
+    for (auto &e : pev) cudaEventDestroy(e);
   }
   cudaEventRecord(e1, h->stream);
   cudaEventSynchronize(e1);

@@ -102,7 +102,7 @@ __global__ void k_hash_insert(const float4 *pos, int n, float ox, float oy, floa
 }
 
 __global__ void k_gather_target(const int *perm, int n, const float4 *pos, const float *feat, int FP, const float *lab,
-                                int CP, const float2 *geo, float4 *tpos, float *tfeat, float *tlab, float2 *tgeo) {
+                                int CP, const float2 *geo, float4 *tpos, float *tfeat, float *tlab, float4 *tgeo) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   int j = perm[t];
@@ -110,7 +110,7 @@ __global__ void k_gather_target(const int *perm, int n, const float4 *pos, const
   tpos[t] = make_float4(p.x, p.y, p.z, __int_as_float(j));
   for (int k = 0; k < FP; k++) tfeat[(size_t)t * FP + k] = feat[(size_t)j * FP + k];
   for (int k = 0; k < CP; k++) tlab[(size_t)t * CP + k] = lab[(size_t)j * CP + k];
-  if (geo) tgeo[t] = geo[j];
+  if (geo) { float2 g = geo[j]; tgeo[t] = make_float4(g.x, g.y, 0.f, 0.f); }
 }
 
 template <typename T>
@@ -136,7 +136,7 @@ int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
   DevCloud *d = new DevCloud();
   d->n = c->n; d->F = c->F; d->C = c->C;
   d->FP = (c->F + 3) / 4 * 4;
-  d->CP = (c->C + 3) / 4 * 4;
+  d->CP = 4 * label_chunks(c->C);
   d->has_geo = c->geom_type != nullptr;
   int n = c->n;
   int rc = 0;
@@ -252,7 +252,7 @@ int cloud_level(Handle *h, DevCloud *d, int e, GridDesc *host_desc) {
   unsigned int *slot_of = nullptr, *slot_tmp = nullptr;
   float4 *tpos = nullptr;
   float *tfeat = nullptr, *tlab = nullptr;
-  float2 *tgeo = nullptr;
+  float4 *tgeo = nullptr;   // 16-byte records so that bulk copies stay aligned
   int rc = 0;
   if ((rc = dalloc(h, &keys, T)) || (rc = dalloc(h, &cstart, T)) || (rc = dalloc(h, &ccount, T)) ||
       (rc = dalloc(h, &perm, n)) || (rc = dalloc(h, &tpos, n)) || (rc = dalloc(h, &tfeat, (size_t)n * d->FP)) ||

@@ -41,7 +41,7 @@ struct GridDesc {
   const float4 *pos;            // sorted copy: x, y, z, original index (int bits)
   const float *feat;            // sorted copy, n * FP
   const float *lab;             // sorted copy, n * CP
-  const float2 *geo;            // sorted copy (may be null)
+  const float4 *geo;            // sorted copy {g0, g1, 0, 0} (may be null)
 };
 
 struct DevCloud {
@@ -92,7 +92,8 @@ struct PairDev {
   int nlevels;
   float level_r[24];              // largest search radius each level serves
   float4 *ycur;                   // transformed targets, current level order
-  int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s]
+  float4 *yorig;                  // transformed targets, original order
+  int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s] (original target index)
   int *nnz_row;                   // n
   float *row_sums;                // n * 8: omega(3)/c, v(3)/d, asum, count
   double *part;                   // reduce partials
@@ -121,7 +122,6 @@ struct PairDev {
   float ssum, esum;
 };
 
-struct OvfEntry { int pair; int row; };
 
 // Batch of pairs processed together by every kernel launch.
 struct BatchDev {
@@ -133,28 +133,42 @@ struct BatchDev {
   const int *tile_off;            // npairs + 1 (prefix of tile counts)
   const int *row_off;             // npairs + 1 (prefix of n)
   const int *tgt_off;             // npairs + 1 (prefix of m)
-  OvfEntry *ovf;                  // overflow list
-  int *ovf_n;                     // overflow count (reset by the transform kernel)
-  int ovf_cap;
   int *err;                       // error word (0 ok)
   const int *rblk_off;            // reduce blocks per pair (prefix)
   const int *sblk_off;            // step blocks per pair (prefix)
   int total_rblocks, total_sblocks;
   int *active;                    // number of pairs not done
+  int *active_iters;              // iterations that started with an active pair
+  double *assoc_bytes;            // algorithmic bytes of the association passes
+  int record_bytes;               // packed bytes of one target record
 };
 
 // ------------------------------------------------------------- host side
 struct Workspace;
 
+struct Profile {
+  bool on = false;
+  double assoc_ms = 0.0;
+  double kernel_ms[5] = {0, 0, 0, 0, 0};   // transform, assoc, reduce, step, all four
+  long long assoc_launches = 0;
+  double assoc_bytes = 0.0;
+  long long iterations = 0;
+};
+
 struct Handle {
   cvo_params params;
   cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  Profile prof;
   int device = 0;
   int num_sms = 0;
   long long launches = 0;
   std::string last_error;
   Workspace *ws = nullptr;
 };
+
+// Label rows are padded to 5 float4 chunks (C <= 20) or 9 chunks (C <= 36).
+inline int label_chunks(int C) { return C <= 0 ? 0 : (C <= 20 ? 5 : (C <= 36 ? 9 : (C + 3) / 4)); }
 
 // grid / cloud management (cvo_grid.cu)
 int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out);

@@ -185,6 +185,25 @@ class CvoGPU:
     def kernel_launches(self) -> int:
         return int(L.lib().cvo_kernel_launch_count(self._h))
 
+    def set_stream(self, stream_ptr: int | None) -> None:
+        """Run the handle's work on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        L.check(L.lib().cvo_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None), "cvo_set_stream")
+
+    def profile(self, on: bool = True) -> None:
+        L.check(L.lib().cvo_profile_enable(self._h, int(on)), "cvo_profile_enable")
+
+    def profile_reset(self) -> None:
+        L.check(L.lib().cvo_profile_reset(self._h), "cvo_profile_reset")
+
+    def profile_read(self) -> dict:
+        ms, n, b, it = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
+        L.check(L.lib().cvo_profile_read(self._h, C.byref(ms), C.byref(n), C.byref(b), C.byref(it)), "cvo_profile_read")
+        k = (C.c_double * 5)()
+        L.check(L.lib().cvo_profile_kernels(self._h, k), "cvo_profile_kernels")
+        names = ("transform", "assoc", "reduce", "step", "iteration")
+        return {"assoc_ms": ms.value, "assoc_launches": n.value, "assoc_bytes": b.value, "iterations": it.value,
+                "kernel_ms": {names[i]: k[i] for i in range(5)}}
+
     def upload(self, cloud: CvoPointCloud) -> GpuCloud:
         return GpuCloud(self, cloud)
 
