@@ -207,6 +207,22 @@ int cvo_function_angle(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt
 int cvo_inner_product_batch_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt,
                                 int n_poses, const float *T, float ell, float *out);
 
+/* Inner product that allocates nothing.  No counterpart in the reference: it
+ * is for callers that cannot allocate device memory when they need the value
+ * (fixed-budget real-time loops, hosts that hand out all device memory from
+ * their own pool, plugins forbidden to call cudaMalloc after start-up).
+ * src_dev / tgt_dev describe DEVICE-resident arrays (same layout as cvo_cloud);
+ * the result (same semantics as cvo_inner_product) is written to the device
+ * float *out_dev on `cuda_stream` (NULL = default stream); the call does not
+ * synchronize.  Its only scratch is a fixed 65,792-byte array inside this
+ * library, so at most 1,048,576 source points per call (else
+ * CVO_ERR_CAPACITY); it costs O(N * M).  All calls share that array: calls
+ * whose kernels overlap on the GPU race and must be ordered by the caller.  The
+ * first call on a device looks the array up with that device current; make it
+ * before any stream capture.  No handle is needed. */
+int cvo_inner_product_noalloc(const cvo_params *p, const cvo_cloud *src_dev, const cvo_cloud *tgt_dev,
+                              const float T[16], float ell, float *out_dev, void *cuda_stream);
+
 /* --------------------------------------------------------- association */
 /* CvoGPU::compute_association_gpu (src/cvo/CvoGPU.cu:1836-1871). */
 int cvo_compute_association(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
