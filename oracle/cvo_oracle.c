@@ -798,3 +798,329 @@ void orc_set_num_threads(int n) {
   (void)n;
 #endif
 }
+
+/* ============================================================ multi-frame */
+/* CvoBatchIRLS::solve (src/cvo/IRLS.cpp:148-367) with the per-edge state of
+ * BinaryStateGPU (src/cvo/IRLS_State_GPU.cu:18-336, IRLS_State_GPU.cpp:10-146).
+ * The nonlinear least-squares solve that the reference delegates to Ceres is
+ * restated as the Levenberg-Marquardt iteration below (Ceres itself is not
+ * available; the GPU path implements the same iteration):
+ *   residual  r = a * |T1 p1 - T2 p2|^2, Jacobian J = [e^T R1, (p1 x R1^T e)^T,
+ *             -e^T R2, -(p2 x R2^T e)^T] with e = T1 p1 - T2 p2 (the analytic
+ *             Jacobian of PairwiseAnalyticalDiffFunctor, IRLS_Cost_CPU.hpp:330-357,
+ *             composed with LocalParameterizationSE3::ComputeJacobian, :55-95)
+ *   cost      1/2 sum r^2;  H = sum J^T J, g = sum J^T r (free frames only)
+ *   step      (H + diag(clamp(diag H, 1e-6, 1e32)) / radius) d = -g, radius0 = 1e4
+ *   accept    rho = (cost - cost_new) / (-(g.d + 1/2 d.H.d)) > 1e-3:
+ *             radius /= max(1/3, 1 - (2 rho - 1)^3), nu = 2; else radius /= nu, nu *= 2
+ *   stop      max|g| <= 1e-5, |d| <= 1e-5 (|x| + 1e-5), |dcost| <= 1e-5 cost, or
+ *             max_num_iterations = multiframe_iterations_per_solve
+ *   retract   T <- T * Exp([u; w]) (LocalParameterizationSE3::Plus, :20-45). */
+
+static void se3_exp_d(const double d[6], double X[12]) {
+  /* Exp_SE3(v, is_wu = false) (src/cvo/LieGroup.cpp:169-192): u = v.head(3), w = v.tail(3) */
+  const double *u = d, *w = d + 3;
+  double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  double A[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0}, A2[9], R[9], J[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) A2[3 * r + c] = A[3 * r] * A[c] + A[3 * r + 1] * A[3 + c] + A[3 * r + 2] * A[6 + c];
+  if (th < (double)ORC_TOLERANCE) {
+    for (int t = 0; t < 9; t++) R[t] = J[t] = (t % 4 == 0) ? 1.0 : 0.0;
+  } else {
+    double s1 = sin(th) / th, c1 = (1.0 - cos(th)) / (th * th), c2 = (th - sin(th)) / (th * th * th);
+    for (int t = 0; t < 9; t++) {
+      double I = (t % 4 == 0) ? 1.0 : 0.0;
+      R[t] = I + s1 * A[t] + c1 * A2[t];
+      J[t] = I + c1 * A[t] + c2 * A2[t];
+    }
+  }
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) X[4 * r + c] = R[3 * r + c];
+    X[4 * r + 3] = J[3 * r] * u[0] + J[3 * r + 1] * u[1] + J[3 * r + 2] * u[2];
+  }
+}
+
+static void pose_compose(const double A[12], const double B[12], double out[12]) {
+  double o[12];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 4; c++) {
+      double s = A[4 * r] * B[c] + A[4 * r + 1] * B[4 + c] + A[4 * r + 2] * B[8 + c];
+      if (c == 3) s += A[4 * r + 3];
+      o[4 * r + c] = s;
+    }
+  }
+  memcpy(out, o, sizeof(o));
+}
+
+/* |log(A^-1 B)| (change_of_all_poses, IRLS.cpp:102-110) */
+static double pose_change(const double A[12], const double B[12]) {
+  double Ai[12];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) Ai[4 * r + c] = A[4 * c + r];
+    Ai[4 * r + 3] = -(A[r] * A[3] + A[4 + r] * A[7] + A[8 + r] * A[11]);
+  }
+  double M[12];
+  pose_compose(Ai, B, M);
+  double R[9] = {M[0], M[1], M[2], M[4], M[5], M[6], M[8], M[9], M[10]}, t[3] = {M[3], M[7], M[11]};
+  return orc_dist_se3(R, t);
+}
+
+typedef struct {
+  int f1, f2;
+  int n;                 /* residuals */
+  float *p1, *p2;        /* local positions, n*3 each */
+  float *a;              /* kernel values */
+} res_edge;
+
+static void lm_eval(int nf, const double *poses, int ne, const res_edge *E, int want, double *H, double *g,
+                    double *cost) {
+  int D = 6 * nf;
+  if (want) { memset(H, 0, sizeof(double) * (size_t)D * D); memset(g, 0, sizeof(double) * D); }
+  double c = 0.0;
+  for (int e = 0; e < ne; e++) {
+    const double *T1 = poses + 12 * E[e].f1, *T2 = poses + 12 * E[e].f2;
+    for (int k = 0; k < E[e].n; k++) {
+      double p1[3] = {E[e].p1[3 * k], E[e].p1[3 * k + 1], E[e].p1[3 * k + 2]};
+      double p2[3] = {E[e].p2[3 * k], E[e].p2[3 * k + 1], E[e].p2[3 * k + 2]};
+      double q1[3], q2[3], ev[3];
+      for (int r = 0; r < 3; r++) {
+        q1[r] = T1[4 * r] * p1[0] + T1[4 * r + 1] * p1[1] + T1[4 * r + 2] * p1[2] + T1[4 * r + 3];
+        q2[r] = T2[4 * r] * p2[0] + T2[4 * r + 1] * p2[1] + T2[4 * r + 2] * p2[2] + T2[4 * r + 3];
+        ev[r] = q1[r] - q2[r];
+      }
+      double a = E[e].a[k];
+      double rr = a * (ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+      c += 0.5 * rr * rr;
+      if (!want) continue;
+      double u1[3], u2[3], J[12];
+      for (int r = 0; r < 3; r++) {
+        u1[r] = T1[r] * ev[0] + T1[4 + r] * ev[1] + T1[8 + r] * ev[2];  /* R1^T e */
+        u2[r] = T2[r] * ev[0] + T2[4 + r] * ev[1] + T2[8 + r] * ev[2];  /* R2^T e */
+      }
+      J[0] = u1[0]; J[1] = u1[1]; J[2] = u1[2];
+      J[3] = p1[1] * u1[2] - p1[2] * u1[1]; J[4] = p1[2] * u1[0] - p1[0] * u1[2]; J[5] = p1[0] * u1[1] - p1[1] * u1[0];
+      J[6] = -u2[0]; J[7] = -u2[1]; J[8] = -u2[2];
+      J[9] = -(p2[1] * u2[2] - p2[2] * u2[1]); J[10] = -(p2[2] * u2[0] - p2[0] * u2[2]); J[11] = -(p2[0] * u2[1] - p2[1] * u2[0]);
+      int off[2] = {6 * E[e].f1, 6 * E[e].f2};
+      for (int a1 = 0; a1 < 12; a1++) {
+        int ia = off[a1 / 6] + a1 % 6;
+        g[ia] += J[a1] * rr;
+        for (int b1 = 0; b1 < 12; b1++) {
+          int ib = off[b1 / 6] + b1 % 6;
+          H[(size_t)ia * D + ib] += J[a1] * J[b1];
+        }
+      }
+    }
+  }
+  *cost = c;
+}
+
+/* dense Cholesky solve of the free-variable system; returns 0 on failure */
+static int chol_solve(int n, double *A, double *b) {
+  for (int j = 0; j < n; j++) {
+    double s = A[(size_t)j * n + j];
+    for (int k = 0; k < j; k++) s -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
+    if (!(s > 0.0)) return 0;
+    double d = sqrt(s);
+    A[(size_t)j * n + j] = d;
+    for (int i = j + 1; i < n; i++) {
+      double t = A[(size_t)i * n + j];
+      for (int k = 0; k < j; k++) t -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+      A[(size_t)i * n + j] = t / d;
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    double t = b[i];
+    for (int k = 0; k < i; k++) t -= A[(size_t)i * n + k] * b[k];
+    b[i] = t / A[(size_t)i * n + i];
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double t = b[i];
+    for (int k = i + 1; k < n; k++) t -= A[(size_t)k * n + i] * b[k];
+    b[i] = t / A[(size_t)i * n + i];
+  }
+  return 1;
+}
+
+/* One Levenberg-Marquardt solve; returns the number of successful steps. */
+static int lm_solve(int nf, double *poses, const unsigned char *hold, int ne, const res_edge *E, int max_iter) {
+  int D = 6 * nf;
+  int *idx = (int *)malloc(sizeof(int) * D);
+  int nfree = 0;
+  for (int f = 0; f < nf; f++)
+    for (int k = 0; k < 6; k++) idx[6 * f + k] = hold[f] ? -1 : nfree++;
+  double *H = (double *)malloc(sizeof(double) * (size_t)D * D), *g = (double *)malloc(sizeof(double) * D);
+  double *A = (double *)malloc(sizeof(double) * (size_t)(nfree > 0 ? nfree : 1) * (nfree > 0 ? nfree : 1));
+  double *b = (double *)malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  double *Hf = (double *)malloc(sizeof(double) * (size_t)(nfree > 0 ? nfree : 1) * (nfree > 0 ? nfree : 1));
+  double *gf = (double *)malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  double *cand = (double *)malloc(sizeof(double) * 12 * nf);
+  double radius = 1e4, nu = 2.0, cost = 0.0;
+  int successes = 0;
+  lm_eval(nf, poses, ne, E, 1, H, g, &cost);
+  for (int it = 0; it < max_iter && nfree > 0; it++) {
+    for (int i = 0; i < D; i++) {
+      if (idx[i] < 0) continue;
+      gf[idx[i]] = g[i];
+      for (int j = 0; j < D; j++)
+        if (idx[j] >= 0) Hf[(size_t)idx[i] * nfree + idx[j]] = H[(size_t)i * D + j];
+    }
+    double gmax = 0.0;
+    for (int i = 0; i < nfree; i++) gmax = fmax(gmax, fabs(gf[i]));
+    if (gmax <= 1e-5) break;
+    memcpy(A, Hf, sizeof(double) * (size_t)nfree * nfree);
+    for (int i = 0; i < nfree; i++) {
+      double dg = Hf[(size_t)i * nfree + i];
+      dg = dg < 1e-6 ? 1e-6 : (dg > 1e32 ? 1e32 : dg);
+      A[(size_t)i * nfree + i] += dg / radius;
+      b[i] = -gf[i];
+    }
+    if (!chol_solve(nfree, A, b)) { radius /= nu; nu *= 2.0; continue; }
+    double dn = 0.0, xn = 0.0;
+    for (int i = 0; i < nfree; i++) dn += b[i] * b[i];
+    for (int t = 0; t < 12 * nf; t++) xn += poses[t] * poses[t];
+    if (sqrt(dn) <= 1e-5 * (sqrt(xn) + 1e-5)) break;
+    double model = 0.0;
+    for (int i = 0; i < nfree; i++) {
+      double hd = 0.0;
+      for (int j = 0; j < nfree; j++) hd += Hf[(size_t)i * nfree + j] * b[j];
+      model += gf[i] * b[i] + 0.5 * b[i] * hd;
+    }
+    model = -model;
+    memcpy(cand, poses, sizeof(double) * 12 * nf);
+    for (int f = 0; f < nf; f++) {
+      if (hold[f]) continue;
+      double d6[6], X[12];
+      for (int k = 0; k < 6; k++) d6[k] = b[idx[6 * f + k]];
+      se3_exp_d(d6, X);
+      pose_compose(poses + 12 * f, X, cand + 12 * f);
+    }
+    double cnew = 0.0;
+    lm_eval(nf, cand, ne, E, 0, NULL, NULL, &cnew);
+    double rho = model > 0.0 ? (cost - cnew) / model : -1.0;
+    if (rho > 1e-3) {
+      memcpy(poses, cand, sizeof(double) * 12 * nf);
+      successes++;
+      double rel = fabs(cost - cnew);
+      double fac = 1.0 - pow(2.0 * rho - 1.0, 3.0);
+      radius = radius / (fac > 1.0 / 3.0 ? fac : 1.0 / 3.0);
+      nu = 2.0;
+      int stop = rel <= 1e-5 * cost;
+      cost = cnew;
+      if (stop) break;
+      lm_eval(nf, poses, ne, E, 1, H, g, &cost);
+    } else {
+      radius /= nu;
+      nu *= 2.0;
+    }
+  }
+  free(idx); free(H); free(g); free(A); free(b); free(Hf); free(gf); free(cand);
+  return successes;
+}
+
+/* float world transform of a frame: ((r0 x + r1 y) + r2 z) + t with float(pose) */
+static void world_points(const double pose[12], const cvo_cloud *c, float *out) {
+  float P[12];
+  for (int t = 0; t < 12; t++) P[t] = (float)pose[t];
+  for (int i = 0; i < c->n; i++) {
+    float x = cloud_x(c, i, 0), y = cloud_x(c, i, 1), z = cloud_x(c, i, 2);
+    for (int r = 0; r < 3; r++) {
+      float a = P[4 * r] * x, b = P[4 * r + 1] * y, cc = P[4 * r + 2] * z;
+      out[3 * (size_t)i + r] = ((a + b) + cc) + P[4 * r + 3];
+    }
+  }
+}
+
+/* Returns the number of outer iterations; poses (nf*12, row-major 3x4 frame->world) in/out. */
+int orc_align_multi(const cvo_params *p, int nf, const cvo_cloud *clouds, double *poses, const unsigned char *hold,
+                    int ne, const int *edges, int *lm_steps_out) {
+  double *ell = (double *)malloc(sizeof(double) * (ne > 0 ? ne : 1));
+  int *nn = (int *)malloc(sizeof(int) * (ne > 0 ? ne : 1));
+  int *prev_max = (int *)calloc((size_t)(ne > 0 ? ne : 1), sizeof(int));
+  long long *prev_nnz = (long long *)calloc((size_t)(ne > 0 ? ne : 1), sizeof(long long));
+  long long *nz_last = (long long *)calloc((size_t)(ne > 0 ? ne : 1), sizeof(long long));
+  int *iters_per_ell = (int *)calloc((size_t)(ne > 0 ? ne : 1), sizeof(int));
+  const int init_nn = p->multiframe_num_neighbors;
+  const float ell_init = p->multiframe_ell_init, ell_min = p->multiframe_ell_min;
+  const double ell_max = (double)ell_init * 1.2;
+  for (int e = 0; e < ne; e++) { ell[e] = ell_init; nn[e] = init_nn; }
+  float **world = (float **)malloc(sizeof(float *) * nf);
+  for (int f = 0; f < nf; f++) world[f] = (float *)malloc(sizeof(float) * 3 * (size_t)(clouds[f].n > 0 ? clouds[f].n : 1));
+  res_edge *E = (res_edge *)calloc((size_t)(ne > 0 ? ne : 1), sizeof(res_edge));
+  double *old = (double *)malloc(sizeof(double) * 12 * nf);
+  double *ell_old = (double *)malloc(sizeof(double) * (ne > 0 ? ne : 1));
+  int iter = 0, steps = 0;
+  for (;;) {
+    memcpy(old, poses, sizeof(double) * 12 * nf);
+    memcpy(ell_old, ell, sizeof(double) * (ne > 0 ? ne : 1));
+    for (int f = 0; f < nf; f++) world_points(poses + 12 * f, &clouds[f], world[f]);
+    int counter = 0, nres_edges = 0;
+    for (int e = 0; e < ne; e++) {
+      int f1 = edges[2 * e], f2 = edges[2 * e + 1];
+      nz_last[e] = prev_nnz[e];
+      if (prev_max[e] > 0) { int c = (int)((double)prev_max[e] * 1.1); nn[e] = init_nn < c ? init_nn : c; }
+      cvo_cloud s = clouds[f1];
+      s.xyz = world[f1];
+      s.xyz_stride = 3;
+      int n1 = s.n, cap = nn[e];
+      int *ind = (int *)malloc(sizeof(int) * (size_t)(n1 > 0 ? n1 : 1) * (cap > 0 ? cap : 1));
+      float *val = (float *)malloc(sizeof(float) * (size_t)(n1 > 0 ? n1 : 1) * (cap > 0 ? cap : 1));
+      int *nz = (int *)malloc(sizeof(int) * (n1 > 0 ? n1 : 1));
+      orc_fill_A(p, &s, &clouds[f2], world[f2], cap, (float)ell[e], ind, val, nz);
+      long long sum = 0; int mx = 0;
+      for (int i = 0; i < n1; i++) { sum += nz[i]; if (nz[i] > mx) mx = nz[i]; }
+      prev_nnz[e] = sum; prev_max[e] = mx;
+      if (sum > p->multiframe_min_nonzeros) counter++;
+      free(E[e].p1); free(E[e].p2); free(E[e].a);
+      E[e].p1 = E[e].p2 = NULL; E[e].a = NULL; E[e].n = 0;
+      E[e].f1 = f1; E[e].f2 = f2;
+      if (sum != 0 && sum >= p->multiframe_min_nonzeros) {
+        int lim = p->nearest_neighbors_max < cap ? p->nearest_neighbors_max : cap;
+        long long tot = 0;
+        for (int i = 0; i < n1; i++) tot += nz[i] < lim ? nz[i] : lim;
+        E[e].p1 = (float *)malloc(sizeof(float) * 3 * (size_t)(tot > 0 ? tot : 1));
+        E[e].p2 = (float *)malloc(sizeof(float) * 3 * (size_t)(tot > 0 ? tot : 1));
+        E[e].a = (float *)malloc(sizeof(float) * (size_t)(tot > 0 ? tot : 1));
+        int k = 0;
+        for (int i = 0; i < n1; i++)
+          for (int t = 0; t < nz[i] && t < lim; t++) {
+            int j = ind[(size_t)i * cap + t];
+            for (int r = 0; r < 3; r++) { E[e].p1[3 * k + r] = cloud_x(&clouds[f1], i, r); E[e].p2[3 * k + r] = cloud_x(&clouds[f2], j, r); }
+            E[e].a[k] = val[(size_t)i * cap + t];
+            k++;
+          }
+        E[e].n = k;
+        nres_edges++;
+      }
+      free(ind); free(val); free(nz);
+    }
+    if (counter == 0) break;
+    steps += lm_solve(nf, poses, hold, ne, E, p->multiframe_iterations_per_solve);
+    double change = 0.0;
+    for (int f = 0; f < nf; f++) change += pose_change(old + 12 * f, poses + 12 * f);
+    int all_min = 1;
+    for (int e = 0; e < ne; e++) {
+      /* BinaryStateGPU::update_ell (IRLS_State_GPU.cpp:117-146) */
+      iters_per_ell[e]++;
+      if (p->multiframe_is_optimizing_ell == 0) {
+        if (nz_last[e] > 0 && prev_nnz[e] <= nz_last[e] && iters_per_ell[e] / p->multiframe_iter_per_ell > 0) {
+          ell[e] = ell[e] * (double)p->multiframe_ell_decay_rate;
+          nz_last[e] = 0;
+          iters_per_ell[e] = 0;
+        }
+      }
+      if (ell[e] < ell_min) ell[e] = ell_min;
+      else if (ell[e] > ell_max) ell[e] = ell_max;
+      all_min = all_min && fabs((double)(float)ell[e] - (double)ell_min) < 1e-4;
+    }
+    iter++;
+    if (all_min && change < 1e-5) break;
+    if (iter >= p->multiframe_max_iters) break;
+  }
+  if (lm_steps_out) *lm_steps_out = steps;
+  for (int e = 0; e < ne; e++) { free(E[e].p1); free(E[e].p2); free(E[e].a); }
+  for (int f = 0; f < nf; f++) free(world[f]);
+  free(world); free(E); free(old); free(ell_old); free(ell); free(nn); free(prev_max); free(prev_nnz); free(nz_last);
+  free(iters_per_ell);
+  return iter;
+}

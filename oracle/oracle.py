@@ -242,3 +242,25 @@ def nearest_init_pose(params, src, tgt, ell, rots):
     bi = _lib().orc_nearest_init_pose(_pp(params), _pc(s), _pc(t), float(ell), rots.ctypes.data_as(_fp), nr,
                                       To.ctypes.data_as(_fp), cos.ctypes.data_as(_fp))
     return bi, To.reshape(4, 4).T.copy(), cos
+
+
+def align_multi(params, clouds, poses, hold_const, edges):
+    """CvoBatchIRLS::solve restated (see oracle/cvo_oracle.c).  poses: (n, 12) row-major
+    3x4 frame->world; returns (poses_out, outer_iterations, lm_successful_steps)."""
+    L = _lib()
+    if not hasattr(L.orc_align_multi, "_bound"):
+        L.orc_align_multi.restype = C.c_int
+        L.orc_align_multi.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint8),
+                                      C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_align_multi._bound = True
+    from rkhs_ba_gb300._lib import CvoCloudC
+    n = len(clouds)
+    cs = (CvoCloudC * n)(*[c.c_struct() for c in clouds])
+    P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(n, 12).copy())
+    hc = np.ascontiguousarray(np.asarray(hold_const, np.uint8).reshape(n))
+    E = np.ascontiguousarray(np.asarray(edges, np.int32).reshape(-1, 2))
+    steps = C.c_int(0)
+    it = L.orc_align_multi(_pp(params), n, C.cast(cs, C.c_void_p), P.ctypes.data_as(C.POINTER(C.c_double)),
+                           hc.ctypes.data_as(C.POINTER(C.c_uint8)), E.shape[0], E.ctypes.data_as(C.POINTER(C.c_int)),
+                           C.byref(steps))
+    return P, it, steps.value

@@ -815,6 +815,54 @@ int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::
   return 0;
 }
 
+int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                          const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
+                          const std::vector<float> &tgt_pose, const std::vector<float> &ells,
+                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out) {
+  const int ne = (int)srcs.size();
+  out->assign(ne, EdgeAssoc());
+  if (ne == 0) return 0;
+  KParams K = make_kparams(h->params);
+  std::vector<float> Tid(16 * (size_t)ne, 0.f);
+  for (int e = 0; e < ne; e++) Tid[16 * e] = Tid[16 * e + 5] = Tid[16 * e + 10] = Tid[16 * e + 15] = 1.f;
+  BatchHost bh;
+  int rc = build_batch(h, K, srcs, tgts, Tid, MODE_EXPORT, capmax, ells, &bh);
+  if (rc) return rc;
+  for (int e = 0; e < ne; e++) {
+    PairDev &P = bh.pairs[e];
+    if (P.done) continue;
+    P.xs = src_world[e];
+    P.cap = caps[e];
+    const float *Q = &tgt_pose[12 * e];
+    for (int r = 0; r < 3; r++) {
+      for (int c = 0; c < 3; c++) P.Ri[3 * r + c] = Q[4 * r + c];   // target moved by its own pose
+      P.Ti[r] = Q[4 * r + 3];
+    }
+    // inverse (only used to place the query box in the target's own frame)
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) P.R[3 * r + c] = Q[4 * c + r];
+    for (int r = 0; r < 3; r++) P.T[r] = -(P.R[3 * r] * Q[3] + P.R[3 * r + 1] * Q[7] + P.R[3 * r + 2] * Q[11]);
+    float rw = host_radius(K, ells[e], src_world_norm[e]);
+    P.level = P.nlevels - 1;
+    for (int i = 0; i < P.nlevels; i++)
+      if (P.level_r[i] >= rw) { P.level = i; break; }
+    P.level_used = P.level;
+  }
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(bh.B.pairs, bh.pairs.data(), sizeof(PairDev) * ne, cudaMemcpyHostToDevice, h->stream));
+  launch_association(h, &bh, K);
+  if ((rc = check_err(h, &bh))) return rc;
+  if ((rc = read_pairs(h, &bh))) return rc;
+  for (int e = 0; e < ne; e++) {
+    const PairDev &P = bh.pairs[e];
+    EdgeAssoc &A = (*out)[e];
+    A.A_j = P.A_j; A.A_v = P.A_v; A.nnz_row = P.nnz_row;
+    A.n = P.n; A.m = P.m;
+    A.nnz = P.done ? 0 : P.nnz_sum;
+    A.max_row = P.done ? 0 : P.max_row;
+  }
+  return 0;
+}
+
 int set_cuda_error(Handle *h, cudaError_t e, const char *where) {
   if (h) {
     h->last_error = std::string(where) + ": " + cudaGetErrorString(e);

@@ -200,6 +200,24 @@ int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::
                             bool export_assoc, std::vector<int> *a_rowptr_host, std::vector<int> *a_cols,
                             std::vector<float> *a_vals);
 
+// One association pass per edge between world-frame clouds (multi-frame solver).
+// src_world: per edge, the source frame's points already in world coordinates in
+// tile order ({x, y, z, ||x||}); tgt_pose: per edge 12 floats, the target frame's
+// pose (row-major 3x4, frame -> world) applied to the target points.  The result
+// arrays stay valid until the next batch is built on the handle.
+struct EdgeAssoc {
+  const int *A_j;        // ELL, slot-major over tile-ordered rows, original target indices
+  const float *A_v;
+  const int *nnz_row;
+  int n, m;
+  long long nnz;
+  int max_row;
+};
+int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                          const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
+                          const std::vector<float> &tgt_pose, const std::vector<float> &ells,
+                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out);
+
 // IRLS (cvo_irls.cu)
 int run_align_multi(Handle *h, int n_frames, DevCloud *const *clouds, double *poses, const uint8_t *hold_const,
                     int n_edges, const int *edges, double *secs, int *iters);
