@@ -21,7 +21,7 @@ namespace {
 constexpr int kChunk = 8;
 
 // ------------------------------------------------------------------ reduce
-// Per-pair FP64 sums of the per-row partials written by k_assoc / k_overflow.
+// Per-pair FP64 sums of the per-row partials written by k_assoc / k_select / k_rescan.
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(BatchDev B, KParams K) {
   __shared__ double sh[kReduceThreads / 32][10];
   __shared__ bool last;
@@ -304,16 +304,34 @@ using AssocFn = void (*)(BatchDev, KParams);
 // Feature rows are stored as ceil(F/4) float4 chunks; label rows as 5 or 9
 // chunks (C <= 20 or C <= 36, padded at upload), so the chunk counts below are
 // the storage strides of the clouds.
-int select_kernels(const KParams &K, int F, int C, AssocFn &a) {
+template <int FC, int LC, bool G>
+static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem) {
+  a = k_assoc<FC, LC, G>;
+  rs = k_rescan<FC, LC, G>;
+  smem = AssocSmem<FC, LC, G>::kBytes;
+  // opt in above the 48 KB default once per device (setting it twice is harmless)
+  static unsigned long long set_mask = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return CVO_ERR_CUDA; }
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(set_mask & bit)) {
+    if (cudaFuncSetAttribute(a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      return CVO_ERR_CUDA;
+    }
+    set_mask |= bit;
+  }
+  return 0;
+}
+
+int select_kernels(const KParams &K, int F, int C, AssocFn &a, AssocFn &rs, size_t &smem) {
   int fch = K.use_int ? (F + 3) / 4 : 0;
   int lch = K.use_sem ? label_chunks(C) : 0;
   bool gt = K.use_gtype != 0;
   if (fch > 2 || lch > 9) return CVO_ERR_UNSUPPORTED;
-#define CVO_PICK(FC, LC)                         \
-  if (fch == FC && lch == LC) {                  \
-    if (gt) a = k_assoc<FC, LC, true>;           \
-    else a = k_assoc<FC, LC, false>;             \
-    return 0;                                    \
+#define CVO_PICK(FC, LC)                                       \
+  if (fch == FC && lch == LC) {                                \
+    return gt ? pick_assoc<FC, LC, true>(a, rs, smem) : pick_assoc<FC, LC, false>(a, rs, smem); \
   }
   CVO_PICK(0, 0) CVO_PICK(1, 0) CVO_PICK(2, 0)
   CVO_PICK(0, 5) CVO_PICK(1, 5) CVO_PICK(2, 5)
@@ -397,6 +415,22 @@ KParams make_kparams(const cvo_params &p) {
   k.use_sem = p.is_using_semantics;
   k.use_gtype = p.is_using_geometric_type;
   k.cell_mult = 1.0f;
+  {
+    float t = 2.f * k.c2;
+    k.inv2c2 = 1.f / t;
+  }
+  // Kernel value bound: a <= sigma^2 c_sigma^2 s_sigma^2 exp(-(d2/(2l^2) + d2c/(2c^2))) (the geometric-type
+  // factor is <= 1), so a > sp_thres needs the exponent below ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres).
+  k.use_mma = 0;
+  k.mma_tau = 0.f;
+  if (k.use_geo && p.sp_thres > 0.f && k.sigma2 > 0.f && (!k.use_int || k.c_sigma2 > 0.f) &&
+      (!k.use_sem || k.s_sigma_sq > 0.f)) {
+    double lb = std::log((double)k.sigma2) - std::log((double)p.sp_thres);
+    if (k.use_int) lb += std::log((double)k.c_sigma2);
+    if (k.use_sem) lb += std::log((double)k.s_sigma_sq);
+    k.mma_tau = (float)(lb + 1e-3);
+    k.use_mma = 1;
+  }
   return k;
 }
 
@@ -416,7 +450,10 @@ struct BatchHost {
   std::vector<PairDev> pairs;
   std::vector<int> tile_off, row_off, tgt_off, rblk_off, sblk_off;
   float *src_max_norm = nullptr;
-  AssocFn assoc = nullptr;
+  AssocFn assoc = nullptr, rescan = nullptr;
+  size_t assoc_smem = 0;
+  int sel_blocks = 0;
+  int ov = 0;
   int assoc_blocks = 0, xform_blocks = 0;
 };
 
@@ -430,7 +467,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     if (srcs[p]->F != F || tgts[p]->F != F || srcs[p]->C != C || tgts[p]->C != C) return CVO_ERR_INVALID_ARG;
     if (K.use_gtype && (!srcs[p]->has_geo || !tgts[p]->has_geo)) return CVO_ERR_INVALID_ARG;
   }
-  int rc = select_kernels(K, F, C, bh->assoc);
+  int rc = select_kernels(K, F, C, bh->assoc, bh->rescan, bh->assoc_smem);
   if (rc) return rc;
   // grid levels per pair
   std::vector<std::vector<GridDesc>> lv(np);
@@ -466,6 +503,12 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
   int max_part_blocks = 0;
+  // overflow entries per row: up to 3 cap, within kSelMax, and at most 4 GB for the batch
+  long long rows_all = 0;
+  for (int p = 0; p < np; p++) rows_all += srcs[p]->n;
+  int ov = std::max(0, std::min(3 * capmax, kSelMax - capmax));
+  if (rows_all > 0) ov = (int)std::min<long long>(ov, (4ll << 30) / (8ll * rows_all));
+  bh->ov = ov;
   for (int p = 0; p < np; p++) {
     int n = srcs[p]->n, m = tgts[p]->n;
     bh->tile_off[p + 1] = bh->tile_off[p] + (n + 31) / 32;
@@ -479,6 +522,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     add(sizeof(float4) * m);                                     // yorig
     add(sizeof(int) * (size_t)n * capmax);                       // ELL (every mode: the row selection uses it)
     add(sizeof(float) * (size_t)n * capmax);
+    add(sizeof(int2) * (size_t)n * ov);                          // overflow entries
     add(sizeof(int) * n);                                        // nnz_row
     add(sizeof(float) * 8 * (size_t)n);                          // row_sums
     add(sizeof(double) * kPartStride * (size_t)std::max(rb, sb)); // partials
@@ -488,8 +532,10 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   const int total_rows = bh->row_off[np];
   add(sizeof(PairDev) * np);
   add(sizeof(int) * (np + 1) * 5);
-  add(sizeof(int) * 4);
+  add(sizeof(int) * 6);
   add(sizeof(float) * np);
+  add(sizeof(int4) * (size_t)total_rows);                        // selection list
+  add(sizeof(int4) * (size_t)total_rows);                        // rescan list
   if ((rc = ensure_workspace(h, bytes))) return rc;
   Arena ar;
   ar.base = h->ws->dev;
@@ -507,6 +553,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     P.yorig = ar.take<float4>(t->n);
     P.A_j = ar.take<int>((size_t)s->n * capmax);
     P.A_v = ar.take<float>((size_t)s->n * capmax);
+    P.ovf = ar.take<int2>((size_t)s->n * ov);
+    P.ov = ov;
+    P.tf = t->feat; P.tl = t->lab; P.tg = t->geo;
     P.nnz_row = ar.take<int>(s->n);
     P.row_sums = ar.take<float>(8 * (size_t)s->n);
     int rb = bh->rblk_off[p + 1] - bh->rblk_off[p], sb = bh->sblk_off[p + 1] - bh->sblk_off[p];
@@ -543,9 +592,11 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   }
   PairDev *pairs_d = ar.take<PairDev>(np);
   int *offs_d = ar.take<int>((size_t)(np + 1) * 5);
-  int *ctr_d = ar.take<int>(4);
+  int *ctr_d = ar.take<int>(6);
   double *bytes_d = ar.take<double>(1);
   bh->src_max_norm = ar.take<float>(np);
+  int4 *sel_list_d = ar.take<int4>(total_rows);
+  int4 *scan_list_d = ar.take<int4>(total_rows);
   // zero counters of every pair
   for (int p = 0; p < np; p++) CVO_CUDA_TRY(h, cudaMemsetAsync(bh->pairs[p].counter, 0, 2 * sizeof(unsigned), h->stream));
   for (auto &u : uploads) CVO_CUDA_TRY(h, cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, h->stream));
@@ -557,7 +608,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   int active = 0;
   for (int p = 0; p < np; p++) { mn[p] = srcs[p]->max_norm; if (!bh->pairs[p].done) active++; }
   CVO_CUDA_TRY(h, cudaMemcpyAsync(bh->src_max_norm, mn.data(), sizeof(float) * np, cudaMemcpyHostToDevice, h->stream));
-  int ctr_h[4] = {0, 0, active, 0};
+  int ctr_h[6] = {0, 0, active, 0, 0, 0};
   CVO_CUDA_TRY(h, cudaMemcpyAsync(ctr_d, ctr_h, sizeof(ctr_h), cudaMemcpyHostToDevice, h->stream));
   CVO_CUDA_TRY(h, cudaMemsetAsync(bytes_d, 0, sizeof(double), h->stream));
   CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -579,12 +630,17 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   B.active = ctr_d + 2;
   B.active_iters = ctr_d + 3;
   B.assoc_bytes = bytes_d;
+  B.sel_list = sel_list_d;
+  B.scan_list = scan_list_d;
+  B.sel_count = ctr_d + 4;
+  B.scan_count = ctr_d + 5;
   {
     int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
     B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
   }
   bh->assoc_blocks = (B.total_warps * 32 + kAssocThreads - 1) / kAssocThreads;
   bh->xform_blocks = (B.total_targets + 255) / 256;
+  bh->sel_blocks = std::max(1, std::min(h->num_sms > 0 ? 4 * h->num_sms : 608, (total_rows + 3) / 4));
   return 0;
 }
 
@@ -600,11 +656,13 @@ void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEv
   mark(h, ev, 0);
   k_transform<<<std::max(bh->xform_blocks, 1), 256, 0, h->stream>>>(B);
   mark(h, ev, 1);
-  bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, 0, h->stream>>>(B, K);
+  bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, bh->assoc_smem, h->stream>>>(B, K);
+  k_select<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
+  bh->rescan<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
   mark(h, ev, 2);
   k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
   mark(h, ev, 3);
-  h->launches += 3;
+  h->launches += 5;
 }
 
 void launch_iteration(Handle *h, BatchHost *bh, const KParams &K, const cudaEvent_t *ev = nullptr) {

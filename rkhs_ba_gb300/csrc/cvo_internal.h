@@ -78,6 +78,11 @@ struct KParams {
   int ell_decay_start, indicator_window_size, max_iter, nn_max, use_range_ell_step;
   int use_geo, use_int, use_sem, use_gtype;
   float cell_mult;       // cell size >= cell_mult * search radius
+  float inv2c2;          // 1 / (2 c_ell^2), rounded once (IEEE division)
+  // Tensor-core prefilter: a kept pair needs d2/(2l^2) + d2c/(2c_ell^2) < mma_tau
+  // (mma_tau = ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres) + slack), see k_assoc.
+  float mma_tau;
+  int use_mma;
 };
 
 // Per-pair device state.  One struct per pair, in device memory.
@@ -94,6 +99,10 @@ struct PairDev {
   float4 *ycur;                   // transformed targets, current level order
   float4 *yorig;                  // transformed targets, original order
   int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s] (original target index)
+  int2 *ovf;                      // kept pairs beyond cap, row-major [s * ov + t] = {j, bits of a}
+  int ov;                         // overflow entries per row
+  const float *tf, *tl;           // target features / labels, original order (float4 chunks)
+  const float2 *tg;               // target geometric types, original order
   int *nnz_row;                   // n
   float *row_sums;                // n * 8: omega(3)/c, v(3)/d, asum, count
   double *part;                   // reduce partials
@@ -141,6 +150,11 @@ struct BatchDev {
   int *active_iters;              // iterations that started with an active pair
   double *assoc_bytes;            // algorithmic bytes of the association passes
   int record_bytes;               // packed bytes of one target record
+  // rows with more than `cap` kept pairs, {pair, row, kept count, 0}; reset by k_transform
+  int4 *sel_list;                 // cap < count <= cap + ov: select among ELL + overflow entries
+  int *sel_count;
+  int4 *scan_list;                // count > cap + ov: index-ordered rescan of the row
+  int *scan_count;
 };
 
 // ------------------------------------------------------------- host side

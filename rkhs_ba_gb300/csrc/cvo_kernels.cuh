@@ -13,6 +13,7 @@
 //                Exp_SEK3 pose update, SE(3) distance, lengthscale schedule, cap update
 //                                                               (CvoGPU.cu:333-544, 547-665, 1339-1433)
 #pragma once
+#include <cuda_fp16.h>
 #include "cvo_device.cuh"
 
 namespace cvo_gb {
@@ -97,7 +98,7 @@ __device__ __forceinline__ bool eval_pair(const KParams &K, int F, int C, bool p
   if (!__any_sync(FULLMASK, pass)) return false;
   // fast FP32 value
   float kf = K.use_geo ? fm(K.sigma2, __expf(fm(-d2, inv2l2))) : 1.f;
-  float ckf = K.use_int ? fm(K.c_sigma2, __expf(fm(-d2c, __frcp_rn(fm(2.f, K.c2))))) : 1.f;
+  float ckf = K.use_int ? fm(K.c_sigma2, __expf(fm(-d2c, K.inv2c2))) : 1.f;
   float skf = K.use_sem ? fm(K.s_sigma_sq, __expf(fm(-d2s, __frcp_rn(fm(fm(2.f, K.s_ell), K.s_ell))))) : 1.f;
   float af = fm(fm(fm(ckf, kf), skf), geo);
   if (pass && fabsf(fs(af, K.sp_thres)) <= kBand * K.sp_thres) af = exact_value(K, l, d2, d2c, d2s, geo);
@@ -143,7 +144,11 @@ __device__ __forceinline__ bool cell_range(const GridDesc &g, float lox, float l
 // scan) and in original order (gathered by index from the ELL rows).
 __global__ void k_transform(BatchDev B) {
   int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gt == 0 && *B.active > 0) *B.active_iters += 1;
+  if (gt == 0) {
+    if (*B.active > 0) *B.active_iters += 1;
+    *B.sel_count = 0;
+    *B.scan_count = 0;
+  }
   if (gt >= B.total_targets) return;
   int p = find_segment(B.tgt_off, B.npairs, gt);
   PairDev *P = &B.pairs[p];
@@ -162,37 +167,17 @@ __global__ void k_transform(BatchDev B) {
 // -------------------------------------------------------- row selection
 // The reference keeps the first `cap` kept pairs of a row in ascending target
 // index (its scan stops at `cap`, src/cvo/CvoGPU.cu:994-996).  Here candidates
-// arrive in grid order, so once a row holds `cap` pairs its ELL row becomes a
-// max-heap keyed by the original target index: a later pair with a smaller
-// index replaces the root.  At the end the row holds exactly the `cap` smallest
-// kept indices, i.e. the reference's set.
+// arrive in grid order, so k_assoc writes the first `cap` kept pairs of a row to
+// its ELL slots and the next `ov` to the row's overflow entries; a row that kept
+// more than `cap` is listed, and k_select (count <= cap + ov) or k_rescan
+// (count > cap + ov) rewrites its ELL row with the `cap` smallest kept indices,
+// i.e. the reference's set.
 struct EllRow {
   int *j;
   float *v;
   size_t stride;
   __device__ __forceinline__ int &J(int c) const { return j[(size_t)c * stride]; }
   __device__ __forceinline__ float &V(int c) const { return v[(size_t)c * stride]; }
-  __device__ void sift_down(int i, int cap, int jn, float vn) const {
-    while (true) {
-      int l = 2 * i + 1;
-      if (l >= cap) break;
-      int c = l;
-      int jc = J(l);
-      if (l + 1 < cap) {
-        int jr = J(l + 1);
-        if (jr > jc) { c = l + 1; jc = jr; }
-      }
-      if (jc <= jn) break;
-      J(i) = jc;
-      V(i) = V(c);
-      i = c;
-    }
-    J(i) = jn;
-    V(i) = vn;
-  }
-  __device__ void heapify(int cap) const {
-    for (int i = cap / 2 - 1; i >= 0; i--) sift_down(i, cap, J(i), V(i));
-  }
 };
 
 // ------------------------------------------------------- candidate staging
@@ -223,6 +208,148 @@ __device__ __forceinline__ void stage_issue(StageBuf<FCH, LCH, GT> &buf, uint64_
   if (GT) bulk_g2s(buf.geo, G.geo + t0, 16u * nk, mbar);
 }
 
+// ------------------------------------------------- tensor-core prefilter
+// A kept pair satisfies  u = g_s |x - y|^2 + c |xc - yc|^2 < tau  with
+// g_s = 1/(2 l_s^2), c = 1/(2 c_ell^2), tau = ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres)
+// (+ slack): the kernel value is at most the product of the three scales times
+// exp(-u), and the geometric-type factor is at most 1.  Around a per-warp centre
+// p (x~ = x - p, y~ = y - p) u is the inner product of two 16-vectors,
+//   A_s = [-2 g x~ | -2 c xc | g | c | g|x~|^2 + c|xc|^2 | -kappa |A_s| | 0]
+//   B_t = [ y~     |  yc     | |y~|^2 | |yc|^2 | 1       |  |B_t|        | 0]
+// so a 32-source x 32-candidate tile of u is a 32x32x16 GEMM.  Each vector is
+// split into f16 hi + lo parts and the tile is Ahi*Bhi + Ahi*Blo + Alo*Bhi
+// (mma.sync m16n8k16, FP32 accumulation): the error is below 2^-16 |A||B|, and
+// the -kappa |A||B| column (kappa = 2^-12) lowers u by more than that, so the
+// test "u < tau" never rejects a pair the exact evaluation keeps.  Only pairs
+// that pass go through the exact per-pair arithmetic (eval_pair), in the same
+// candidate order as an unfiltered scan, so the kernel matrix is unchanged.
+constexpr float kMmaKappa = 1.f / 4096.f;
+constexpr float kMmaMaxAbs = 6.0e4f;    // larger components would leave the f16 range: no filtering
+
+struct __align__(16) MmaTile {
+  uint4 a[4][32];   // source rows:  [hi k0-7, hi k8-15, lo k0-7, lo k8-15][row]
+  uint4 b[4][32];   // candidates:   same layout
+};
+
+__device__ __forceinline__ float f4_at(const float4 &v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// Splits v into f16 hi + lo and stores entry `idx` of the 4 planes; returns false
+// if a component is outside the f16-safe range (or not finite).
+__device__ __forceinline__ bool mma_store_vec(const float (&v)[16], uint4 (*dst)[32], int idx) {
+  uint32_t hw[8], lw[8];
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    float v0 = v[2 * i], v1 = v[2 * i + 1];
+    ok = ok && (fabsf(v0) <= kMmaMaxAbs) && (fabsf(v1) <= kMmaMaxAbs);
+    __half h0 = __float2half_rn(v0), h1 = __float2half_rn(v1);
+    __half l0 = __float2half_rn(v0 - __half2float(h0)), l1 = __float2half_rn(v1 - __half2float(h1));
+    hw[i] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
+    lw[i] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
+  }
+  dst[0][idx] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  dst[1][idx] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+  dst[2][idx] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  dst[3][idx] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+  return ok;
+}
+
+__device__ __forceinline__ void ldsm_x4(const void *p, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_addr(p))
+               : "memory");
+}
+
+__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// A fragments (rows 16m..16m+15) of plane pair `base` (0 = hi, 2 = lo).
+__device__ __forceinline__ void mma_load_a(const MmaTile &T, int base, int m, int lane, uint32_t (&a)[4]) {
+  const int mi = lane >> 3, r8 = lane & 7;
+  ldsm_x4(&T.a[base + (mi >> 1)][16 * m + 8 * (mi & 1) + r8], a[0], a[1], a[2], a[3]);
+}
+
+// B fragments of candidate groups 2j and 2j+1 (candidates 16j..16j+15).
+__device__ __forceinline__ void mma_load_b(const MmaTile &T, int base, int j, int lane, uint32_t (&b)[4]) {
+  const int mi = lane >> 3, r8 = lane & 7;
+  ldsm_x4(&T.b[base + (mi & 1)][16 * j + 8 * (mi >> 1) + r8], b[0], b[1], b[2], b[3]);
+}
+
+// u-tile of the warp's 32 rows against the 32 staged candidates; returns, for the
+// lane's own row, the bit mask of candidates with u < tau.  All lanes call it.
+__device__ __forceinline__ uint32_t mma_filter(const MmaTile &T, int lane, float tau) {
+  uint32_t word = 0;   // byte (2m + h), bit (2n + jj): row 16m + 8h + lane/4, column 8n + 2(lane%4) + jj
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    uint32_t bh[4], bl[4];
+    mma_load_b(T, 0, j, lane, bh);
+    mma_load_b(T, 2, j, lane, bl);
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      uint32_t ah[4], al[4];
+      mma_load_a(T, 0, m, lane, ah);
+      mma_load_a(T, 2, m, lane, al);
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int n = 2 * j + q;
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_16816(d, ah, bh[2 * q], bh[2 * q + 1]);
+        mma_16816(d, ah, bl[2 * q], bl[2 * q + 1]);
+        mma_16816(d, al, bh[2 * q], bh[2 * q + 1]);
+        word |= (d[0] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n);
+        word |= (d[1] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n + 1);
+        word |= (d[2] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n);
+        word |= (d[3] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n + 1);
+      }
+    }
+  }
+  // gather the lane's row: held by lanes 4 (row % 8) + t, t = 0..3
+  const int sh = 8 * (2 * (lane >> 4) + ((lane >> 3) & 1));
+  const int src0 = 4 * (lane & 7);
+  uint32_t mask = 0;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const uint32_t w = __shfl_sync(FULLMASK, word, src0 + t);
+    const uint32_t b = (w >> sh) & 0xFFu;
+    const uint32_t s = (b & 0x3u) | ((b & 0xCu) << 6) | ((b & 0x30u) << 12) | ((b & 0xC0u) << 18);
+    mask |= s << (2 * t);
+  }
+  return mask;
+}
+
+// Row partials as k_reduce reads them: omega / c, v / d (align mode only), sum of a.
+__device__ __forceinline__ void write_row_sums(float *rs, int mode, const KParams &K, float w0, float w1, float w2,
+                                               float v0, float v1, float v2, float as) {
+  if (mode == MODE_ALIGN) {
+    rs[0] = __fdiv_rn(w0, K.c); rs[1] = __fdiv_rn(w1, K.c); rs[2] = __fdiv_rn(w2, K.c);
+    rs[3] = __fdiv_rn(v0, K.d); rs[4] = __fdiv_rn(v1, K.d); rs[5] = __fdiv_rn(v2, K.d);
+  } else {
+    rs[0] = rs[1] = rs[2] = rs[3] = rs[4] = rs[5] = 0.f;
+  }
+  rs[6] = as;
+}
+
+// Dynamic shared memory of one k_assoc block: per warp two staging buffers, the
+// prefilter tile, the grid descriptor and two mbarriers (16-byte aligned pieces).
+template <int FCH, int LCH, bool GT>
+struct AssocSmem {
+  static constexpr int kWarps = kAssocThreads / 32;
+  static constexpr size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+  static constexpr size_t kStage = 0;
+  static constexpr size_t kMma = align16(kStage + sizeof(StageBuf<FCH, LCH, GT>) * 2 * kWarps);
+  static constexpr size_t kGrid = align16(kMma + sizeof(MmaTile) * kWarps);
+  static constexpr size_t kMbar = align16(kGrid + sizeof(GridDesc) * kWarps);
+  static constexpr size_t kBytes = align16(kMbar + sizeof(uint64_t) * 2 * kWarps);
+};
+
 // ------------------------------------------------------------ association
 // One warp per tile of 32 spatially adjacent source points (Morton order).  The
 // warp scans the grid cells overlapping the union of its lanes' query boxes;
@@ -232,13 +359,17 @@ __device__ __forceinline__ void stage_issue(StageBuf<FCH, LCH, GT> &buf, uint64_
 template <int FCH, int LCH, bool GT>
 __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) {
   using Buf = StageBuf<FCH, LCH, GT>;
+  using L = AssocSmem<FCH, LCH, GT>;
   constexpr int CH = Buf::CH;
-  __shared__ Buf stage_all[kAssocThreads / 32][2];
-  __shared__ __align__(8) uint64_t mbar_all[kAssocThreads / 32][2];
-  __shared__ GridDesc grid_all[kAssocThreads / 32];
+  extern __shared__ __align__(128) unsigned char assoc_smem[];
+  Buf(*stage_all)[2] = reinterpret_cast<Buf(*)[2]>(assoc_smem + L::kStage);
+  MmaTile *mma_all = reinterpret_cast<MmaTile *>(assoc_smem + L::kMma);
+  GridDesc *grid_all = reinterpret_cast<GridDesc *>(assoc_smem + L::kGrid);
+  uint64_t(*mbar_all)[2] = reinterpret_cast<uint64_t(*)[2]>(assoc_smem + L::kMbar);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   Buf *stage = stage_all[wib];
+  MmaTile &mt = mma_all[wib];
   uint64_t *mbar = mbar_all[wib];
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= B.total_warps) return;
@@ -301,12 +432,65 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
   // than the lanes' own boxes together, one pass per lane over its own box.
   const bool per_lane = union_cells > 64 && union_cells > 2 * own_sum;
   const int npass = per_lane ? 32 : (union_ok ? 1 : 0);
+  // Tensor-core prefilter for the tile (one pass over the union box, F <= 8).
+  bool use_mma = K.use_mma && npass == 1 && !per_lane && F <= 8;
+  float pcx = 0.f, pcy = 0.f, pcz = 0.f;   // centre of the tile's valid source points
+  const float cw = K.use_int ? K.inv2c2 : 0.f;
+  if (use_mma) {
+    const int nv = warp_sumi(valid ? 1 : 0);
+    const float inv = 1.f / (float)max(nv, 1);
+    pcx = warp_sumf(valid ? x.x : 0.f) * inv;
+    pcy = warp_sumf(valid ? x.y : 0.f) * inv;
+    pcz = warp_sumf(valid ? x.z : 0.f) * inv;
+    float av[16];
+    const float tx = x.x - pcx, ty = x.y - pcy, tz = x.z - pcz;
+    const float g = valid ? rc.inv2l2 : 0.f;
+    av[0] = -2.f * g * tx; av[1] = -2.f * g * ty; av[2] = -2.f * g * tz;
+    float xc2 = 0.f;
+#pragma unroll
+    for (int f = 0; f < 8; f++) {
+      float xv = 0.f;
+      if (FCH > 0 && (f >> 2) < FCH && f < F) xv = f4_at(xf[(f >> 2) < FCH ? (f >> 2) : 0], f & 3);
+      av[3 + f] = valid ? -2.f * cw * xv : 0.f;
+      xc2 += xv * xv;
+    }
+    av[11] = g;
+    av[12] = valid ? cw : 0.f;
+    av[13] = valid ? g * (tx * tx + ty * ty + tz * tz) + cw * xc2 : 0.f;
+    float na = 0.f;
+#pragma unroll
+    for (int k = 0; k < 14; k++) na += av[k] * av[k];
+    av[14] = -kMmaKappa * sqrtf(na);
+    av[15] = 0.f;
+    const bool ok = mma_store_vec(av, mt.a, lane);
+    use_mma = __all_sync(FULLMASK, ok);
+    __syncwarp();
+  }
   int cnt = 0;
-  int root_j = 0x7FFFFFFF;   // largest kept index once the row is a heap
   float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
   const float4 *__restrict__ ycur = P->ycur;
   const EllRow row{P->A_j + (valid ? s : 0), P->A_v + (valid ? s : 0), (size_t)n};
+  const int ov = P->ov;
+  int2 *const ovf_row = P->ovf + (valid ? (size_t)s * ov : 0);
   bool lost = false;
+  // a kept pair enters the row: ELL slot (first cap, with the partial sums) or overflow entry
+  auto keep = [&](float a, const float4 &y) {
+    const int j = __float_as_int(y.w);
+    if (cnt < cap) {
+      row.J(cnt) = j;
+      row.V(cnt) = a;
+      w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
+      w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
+      w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
+      v0 = fmaf(a, y.x - x.x, v0);
+      v1 = fmaf(a, y.y - x.y, v1);
+      v2 = fmaf(a, y.z - x.z, v2);
+      as += a;
+    } else if (cnt - cap < ov) {
+      ovf_row[cnt - cap] = make_int2(j, __float_as_int(a));
+    }
+    cnt++;
+  };
   for (int pass = 0; pass < npass && !lost; pass++) {
     int x0, y0, z0, nx, ny, nz;
     bool me = valid;
@@ -366,35 +550,56 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
           break;
         }
         const Buf &sb = stage[cur];
-        for (int k = 0; k < nk; k++) {
-          const float4 y = sb.pos[k];
-          float a;
-          bool acc = eval_pair<FCH, LCH, GT>(K, F, C, me, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y,
-                                             &sb.feat[k * (FCH > 0 ? FCH : 1)], &sb.lab[k * (LCH > 0 ? LCH : 1)],
-                                             &sb.geo[GT ? k : 0], a);
-          if (acc) {
-            const int j = __float_as_int(y.w);
-            if (cnt < cap) {
-              row.J(cnt) = j;
-              row.V(cnt) = a;
-              w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
-              w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
-              w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
-              v0 = fmaf(a, y.x - x.x, v0);
-              v1 = fmaf(a, y.y - x.y, v1);
-              v2 = fmaf(a, y.z - x.z, v2);
-              as += a;
-            } else if (cap > 0) {
-              if (cnt == cap) {
-                row.heapify(cap);
-                root_j = row.J(0);
-              }
-              if (j < root_j) {
-                row.sift_down(0, cap, j, a);
-                root_j = row.J(0);
-              }
+        if (use_mma) {
+          // candidate vectors of this chunk (lane k builds candidate k; empty slots are zero)
+          float bv[16];
+#pragma unroll
+          for (int q = 0; q < 16; q++) bv[q] = 0.f;
+          if (lane < nk) {
+            const float4 y = sb.pos[lane];
+            bv[0] = y.x - pcx; bv[1] = y.y - pcy; bv[2] = y.z - pcz;
+            float yc2 = 0.f;
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+              float yv = 0.f;
+              if (FCH > 0 && (f >> 2) < FCH && f < F)
+                yv = f4_at(sb.feat[lane * (FCH > 0 ? FCH : 1) + ((f >> 2) < FCH ? (f >> 2) : 0)], f & 3);
+              bv[3 + f] = yv;
+              yc2 += yv * yv;
             }
-            cnt++;
+            bv[11] = bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2];
+            bv[12] = yc2;
+            bv[13] = 1.f;
+            float nb = 0.f;
+#pragma unroll
+            for (int q = 0; q < 14; q++) nb += bv[q] * bv[q];
+            bv[14] = sqrtf(nb);
+          }
+          const bool ok = __all_sync(FULLMASK, mma_store_vec(bv, mt.b, lane));
+          __syncwarp();
+          uint32_t cand = ok ? mma_filter(mt, lane, K.mma_tau) : 0xFFFFFFFFu;
+          cand &= (nk >= 32) ? 0xFFFFFFFFu : ((1u << nk) - 1u);
+          if (!me) cand = 0u;
+          // exact evaluation of the surviving pairs, ascending candidate order per row
+          while (__any_sync(FULLMASK, cand != 0u)) {
+            const bool pre = cand != 0u;
+            const int k = pre ? __ffs(cand) - 1 : 0;
+            cand &= cand - 1u;
+            const float4 y = sb.pos[k];
+            float a;
+            bool acc = eval_pair<FCH, LCH, GT>(K, F, C, pre, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y,
+                                               &sb.feat[k * (FCH > 0 ? FCH : 1)], &sb.lab[k * (LCH > 0 ? LCH : 1)],
+                                               &sb.geo[GT ? k : 0], a);
+            if (acc) keep(a, y);
+          }
+        } else {
+          for (int k = 0; k < nk; k++) {
+            const float4 y = sb.pos[k];
+            float a;
+            bool acc = eval_pair<FCH, LCH, GT>(K, F, C, me, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y,
+                                               &sb.feat[k * (FCH > 0 ? FCH : 1)], &sb.lab[k * (LCH > 0 ? LCH : 1)],
+                                               &sb.geo[GT ? k : 0], a);
+            if (acc) keep(a, y);
           }
         }
         __syncwarp();
@@ -407,32 +612,144 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
     }
   }
   if (valid && !lost) {
-    if (cnt > cap && cap > 0) {
-      // the row overflowed: its sums come from the selected entries
-      const float4 *__restrict__ yorig = P->yorig;
-      w0 = w1 = w2 = v0 = v1 = v2 = as = 0.f;
-      for (int c = 0; c < cap; c++) {
-        float a = row.V(c);
-        float4 y = __ldg(&yorig[row.J(c)]);
-        w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
-        w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
-        w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
-        v0 = fmaf(a, y.x - x.x, v0);
-        v1 = fmaf(a, y.y - x.y, v1);
-        v2 = fmaf(a, y.z - x.z, v2);
-        as += a;
-      }
-    }
-    int kept = cnt < cap ? cnt : cap;
+    const int kept = cnt < cap ? cnt : cap;
     P->nnz_row[s] = kept;
     float *rs = P->row_sums + (size_t)s * 8;
-    if (mode == MODE_ALIGN) {
-      rs[0] = __fdiv_rn(w0, K.c); rs[1] = __fdiv_rn(w1, K.c); rs[2] = __fdiv_rn(w2, K.c);
-      rs[3] = __fdiv_rn(v0, K.d); rs[4] = __fdiv_rn(v1, K.d); rs[5] = __fdiv_rn(v2, K.d);
-    } else {
-      rs[0] = rs[1] = rs[2] = rs[3] = rs[4] = rs[5] = 0.f;
+    write_row_sums(rs, mode, K, w0, w1, w2, v0, v1, v2, as);
+    if (cnt > cap && cap > 0) {
+      // more than cap kept pairs: the row's set is finished by k_select / k_rescan
+      if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
+      else B.scan_list[atomicAdd(B.scan_count, 1)] = make_int4(p, s, cnt, 0);
     }
-    rs[6] = as;
+  }
+}
+
+// ------------------------------------------------------------ selection
+constexpr int kSelMax = 2048;      // ELL + overflow entries one row can hold (cap + ov)
+constexpr int kSelThreads = 128;
+
+// Partial sums of kept pairs of source point x over one warp: per-lane FP32 sums,
+// then a fixed-order warp tree (deterministic).
+struct RowAcc {
+  float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
+  __device__ __forceinline__ void add(const float4 &x, const float4 &y, float a) {
+    w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
+    w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
+    w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
+    v0 = fmaf(a, y.x - x.x, v0);
+    v1 = fmaf(a, y.y - x.y, v1);
+    v2 = fmaf(a, y.z - x.z, v2);
+    as += a;
+  }
+  __device__ __forceinline__ void write(float *rs, int mode, const KParams &K, int lane) {
+    w0 = warp_sumf(w0); w1 = warp_sumf(w1); w2 = warp_sumf(w2);
+    v0 = warp_sumf(v0); v1 = warp_sumf(v1); v2 = warp_sumf(v2); as = warp_sumf(as);
+    if (lane == 0) write_row_sums(rs, mode, K, w0, w1, w2, v0, v1, v2, as);
+  }
+};
+
+// One warp per listed row with cap < count <= cap + ov: the row's cap ELL entries
+// and its overflow entries hold every kept pair; the cap-th smallest target index
+// is found by a bitwise search of counts, and the entries with index up to it
+// (exactly cap, indices are distinct) are compacted into the ELL slots in entry order.
+__global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
+  __shared__ int jbuf_all[kSelThreads / 32][kSelMax];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int *jb = jbuf_all[w];
+  const int count = *B.sel_count;
+  const int nwarps = gridDim.x * (kSelThreads / 32);
+  for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
+    const int4 it = B.sel_list[e];
+    const PairDev *P = &B.pairs[it.x];
+    const int s = it.y, n = P->n, cap = P->cap, ov = P->ov;
+    const int E = cap + min(it.z - cap, ov);
+    const int2 *ovf = P->ovf + (size_t)s * ov;
+    for (int t = lane; t < E; t += 32) jb[t] = t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
+    __syncwarp();
+    // r = largest value with #{j < r} < cap, i.e. the cap-th smallest index
+    int r = 0;
+    for (int b = kMaxTargetBits - 1; b >= 0; b--) {
+      const int tv = r | (1 << b);
+      int c = 0;
+      for (int t = lane; t < E; t += 32) c += jb[t] < tv ? 1 : 0;
+      if (warp_sumi(c) < cap) r = tv;
+    }
+    const float4 x = P->xs[s];
+    RowAcc acc;
+    int base = 0;
+    for (int t0 = 0; t0 < E; t0 += 32) {
+      const int t = t0 + lane;
+      int j = 0;
+      float a = 0.f;
+      bool k = false;
+      if (t < E) {
+        j = jb[t];
+        k = j <= r;
+        a = t < cap ? P->A_v[(size_t)t * n + s] : __int_as_float(ovf[t - cap].y);
+      }
+      const unsigned bal = __ballot_sync(FULLMASK, k);
+      if (k) {
+        const int c = base + __popc(bal & ((1u << lane) - 1u));
+        P->A_j[(size_t)c * n + s] = j;
+        P->A_v[(size_t)c * n + s] = a;
+        acc.add(x, __ldg(&P->yorig[j]), a);
+      }
+      base += __popc(bal);
+    }
+    acc.write(P->row_sums + (size_t)s * 8, P->mode, K, lane);
+    __syncwarp();
+  }
+}
+
+// One warp per listed row with count > cap + ov: the reference's own order, i.e. a
+// scan of the targets by ascending original index (32 per step, one per lane) that
+// stops once cap pairs are kept.  Same per-pair arithmetic as k_assoc.
+template <int FCH, int LCH, bool GT>
+__global__ void __launch_bounds__(kSelThreads) k_rescan(BatchDev B, KParams K) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int count = *B.scan_count;
+  const int nwarps = gridDim.x * (kSelThreads / 32);
+  for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
+    const int4 it = B.scan_list[e];
+    const PairDev *P = &B.pairs[it.x];
+    const int s = it.y, n = P->n, m = P->m, cap = P->cap, F = P->F, C = P->C;
+    const float4 x = P->xs[s];
+    float4 xf[FCH > 0 ? FCH : 1];
+    float4 xl[LCH > 0 ? LCH : 1];
+#pragma unroll
+    for (int q = 0; q < (FCH > 0 ? FCH : 1); q++)
+      xf[q] = FCH > 0 ? __ldg(reinterpret_cast<const float4 *>(P->xf) + (size_t)s * FCH + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < (LCH > 0 ? LCH : 1); q++)
+      xl[q] = LCH > 0 ? __ldg(reinterpret_cast<const float4 *>(P->xl) + (size_t)s * LCH + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 xg = GT ? __ldg(&P->xg[s]) : make_float2(0.f, 0.f);
+    const float Tn = fabsf(P->T[0]) + fabsf(P->T[1]) + fabsf(P->T[2]);
+    const RowConst rc = row_const(K, P->ell, x.w, Tn);
+    RowAcc acc;
+    int taken = 0;
+    for (int j0 = 0; j0 < m && taken < cap; j0 += 32) {
+      const int j = j0 + lane;
+      const bool pre = j < m;
+      const int jj = pre ? j : 0;
+      const float4 y = __ldg(&P->yorig[jj]);
+      float4 yg = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (GT) { const float2 g2 = __ldg(&P->tg[jj]); yg.x = g2.x; yg.y = g2.y; }
+      const float4 *yfp = reinterpret_cast<const float4 *>(P->tf) + (size_t)jj * (FCH > 0 ? FCH : 1);
+      const float4 *ylp = reinterpret_cast<const float4 *>(P->tl) + (size_t)jj * (LCH > 0 ? LCH : 1);
+      float a = 0.f;
+      const bool k = eval_pair<FCH, LCH, GT>(K, F, C, pre, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y, yfp, ylp, &yg, a);
+      const unsigned bal = __ballot_sync(FULLMASK, k);
+      if (k) {
+        const int c = taken + __popc(bal & ((1u << lane) - 1u));
+        if (c < cap) {
+          P->A_j[(size_t)c * n + s] = j;
+          P->A_v[(size_t)c * n + s] = a;
+          acc.add(x, y, a);
+        }
+      }
+      taken += __popc(bal);
+    }
+    acc.write(P->row_sums + (size_t)s * 8, P->mode, K, lane);
   }
 }
 
