@@ -414,7 +414,6 @@ KParams make_kparams(const cvo_params &p) {
   k.use_int = p.is_using_intensity;
   k.use_sem = p.is_using_semantics;
   k.use_gtype = p.is_using_geometric_type;
-  k.cell_mult = 1.0f;
   {
     float t = 2.f * k.c2;
     k.inv2c2 = 1.f / t;
@@ -433,6 +432,13 @@ KParams make_kparams(const cvo_params &p) {
   }
   return k;
 }
+
+// Cell size for search radius r and source tiles of diagonal ext: small against r
+// (the distance test on cells then trims the query box towards the union of balls)
+// while keeping a tile's box at about 8 cells per axis.
+static float cell_for_radius(float r, float ext) { return std::max(0.25f * r, 0.125f * (ext + 2.f * r)); }
+// Largest radius a cell of size hc serves (inverse of cell_for_radius).
+static float radius_for_cell(float hc, float ext) { return std::max(0.f, std::min(4.f * hc, 0.5f * (8.f * hc - ext))); }
 
 static float host_range_ell(float ell, float dist) { return (float)(((double)dist / 500.0 + 1.0) * (double)ell); }
 static float host_radius(const KParams &K, float ell, float norm) {
@@ -474,7 +480,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   std::vector<std::vector<float>> lr(np);
   for (int p = 0; p < np; p++) {
     DevCloud *t = tgts[p];
-    float cm = K.cell_mult;
+    const float ext = srcs[p]->tile_ext;
     std::vector<int> exps;
     if (!K.use_geo) {
       exps.push_back(1000);
@@ -483,7 +489,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
       float ell_lo = (mode == MODE_ALIGN) ? std::min(K.ell_min, ell_hi) : ell_hi;
       float r_hi = host_radius(K, ell_hi, srcs[p]->max_norm);
       float r_lo = host_radius(K, ell_lo, 0.f);
-      int e_hi = level_for_radius(cm * r_hi), e_lo = level_for_radius(cm * r_lo);
+      int e_hi = level_for_radius(cell_for_radius(r_hi, ext)), e_lo = level_for_radius(cell_for_radius(r_lo, ext));
       if (e_hi - e_lo + 1 > 24) e_lo = e_hi - 23;
       for (int e = e_lo; e <= e_hi; e++) exps.push_back(e);
     }
@@ -491,7 +497,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
       GridDesc g;
       if ((rc = cloud_level(h, t, e, &g))) return rc;
       lv[p].push_back(g);
-      lr[p].push_back(e >= 1000 ? INFINITY : (float)(g.h / cm));
+      lr[p].push_back(e >= 1000 ? INFINITY : radius_for_cell(g.h, ext));
     }
   }
   // sizes
@@ -659,10 +665,11 @@ void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEv
   bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, bh->assoc_smem, h->stream>>>(B, K);
   k_select<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
   bh->rescan<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
+  k_rowsum<<<std::max((B.total_rows + 255) / 256, 1), 256, 0, h->stream>>>(B, K);
   mark(h, ev, 2);
   k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
   mark(h, ev, 3);
-  h->launches += 5;
+  h->launches += 6;
 }
 
 void launch_iteration(Handle *h, BatchHost *bh, const KParams &K, const cudaEvent_t *ev = nullptr) {

@@ -63,6 +63,27 @@ __global__ void k_morton(const float4 *pos, int n, float ox, float oy, float oz,
   vals[i] = i;
 }
 
+// Bounding-box diagonal of each 32-point tile (one warp per tile).
+__global__ void k_tile_extent(const float4 *spos, int n, float *ext) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tile = g >> 5, lane = g & 31;
+  const int tiles = (n + 31) / 32;
+  if (tile >= tiles) return;
+  const int s = tile * 32 + lane;
+  float4 p = s < n ? spos[s] : spos[tile * 32];
+  float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z};
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+      hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+    }
+  }
+  if (lane == 0) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    ext[tile] = sqrtf(dx * dx + dy * dy + dz * dz);
+  }
+}
+
 __global__ void k_gather_source(const int *perm, int n, const float4 *pos, const float *feat, int FP, const float *lab,
                                 int CP, const float2 *geo, float4 *spos, float *sfeat, float *slab, float2 *sgeo) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -207,7 +228,17 @@ int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
   k_gather_source<<<(n + 255) / 256, 256, 0, h->stream>>>(d->sperm, n, d->pos, d->feat, d->FP, d->lab, d->CP, d->geo,
                                                          d->spos, d->sfeat, d->slab, d->sgeo);
   h->launches++;
+  // mean bounding-box diagonal of the 32-point source tiles (sizes the grid cells)
+  const int tiles = (n + 31) / 32;
+  float *ext_d = reinterpret_cast<float *>(keys);
+  k_tile_extent<<<(tiles * 32 + 255) / 256, 256, 0, h->stream>>>(d->spos, n, ext_d);
+  h->launches++;
+  std::vector<float> ext_h(tiles);
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(ext_h.data(), ext_d, sizeof(float) * tiles, cudaMemcpyDeviceToHost, h->stream));
   CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  double es = 0.0;
+  for (float e : ext_h) es += e;
+  d->tile_ext = tiles > 0 ? (float)(es / tiles) : 0.f;
   cudaFree(xyz_d); cudaFree(feat_in); cudaFree(lab_in);
   cudaFree(keys); cudaFree(keys_tmp); cudaFree(perm_vals); cudaFree(perm_tmp);
   return 0;

@@ -49,6 +49,7 @@ struct DevCloud {
   bool has_geo = false;
   float bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
   float max_norm = 0.f;
+  float tile_ext = 0.f;          // mean bounding-box diagonal of the 32-point source tiles
   // original order
   float4 *pos = nullptr;
   float *feat = nullptr;
@@ -77,7 +78,6 @@ struct KParams {
   float ell_decay_rate, ell_min, indicator_stable_threshold;
   int ell_decay_start, indicator_window_size, max_iter, nn_max, use_range_ell_step;
   int use_geo, use_int, use_sem, use_gtype;
-  float cell_mult;       // cell size >= cell_mult * search radius
   float inv2c2;          // 1 / (2 c_ell^2), rounded once (IEEE division)
   // Tensor-core prefilter: a kept pair needs d2/(2l^2) + d2c/(2c_ell^2) < mma_tau
   // (mma_tau = ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres) + slack), see k_assoc.

@@ -195,17 +195,23 @@ struct __align__(16) StageBuf {
 };
 
 template <int FCH, int LCH, bool GT>
-__device__ __forceinline__ void stage_issue(StageBuf<FCH, LCH, GT> &buf, uint64_t *mbar, const float4 *ycur,
-                                            const GridDesc &G, int t0, int nk) {
-  constexpr uint32_t rec = 16u * (1 + FCH + LCH + (GT ? 1 : 0));
-  fence_proxy_async_smem();   // the lanes' reads of this buffer precede the copy into it
-  mbar_arrive_expect_tx(mbar, rec * (uint32_t)nk);
-  bulk_g2s(buf.pos, ycur + t0, 16u * nk, mbar);
+struct StageRec {
+  static constexpr uint32_t kBytes = 16u * (1 + FCH + LCH + (GT ? 1 : 0));   // staged bytes per candidate
+};
+
+// Copies `nk` grid-order candidates starting at t0 into slots [at, at + nk) of a
+// staging buffer (positions, features, labels, geometric types), completing on mbar.
+template <int FCH, int LCH, bool GT>
+__device__ __forceinline__ void stage_piece(StageBuf<FCH, LCH, GT> &buf, uint64_t *mbar, const float4 *ycur,
+                                            const GridDesc &G, int at, int t0, int nk) {
+  bulk_g2s(buf.pos + at, ycur + t0, 16u * nk, mbar);
   if (FCH > 0)
-    bulk_g2s(buf.feat, reinterpret_cast<const float4 *>(G.feat) + (size_t)t0 * FCH, 16u * FCH * nk, mbar);
+    bulk_g2s(buf.feat + (size_t)at * FCH, reinterpret_cast<const float4 *>(G.feat) + (size_t)t0 * FCH,
+             16u * FCH * nk, mbar);
   if (LCH > 0)
-    bulk_g2s(buf.lab, reinterpret_cast<const float4 *>(G.lab) + (size_t)t0 * LCH, 16u * LCH * nk, mbar);
-  if (GT) bulk_g2s(buf.geo, G.geo + t0, 16u * nk, mbar);
+    bulk_g2s(buf.lab + (size_t)at * LCH, reinterpret_cast<const float4 *>(G.lab) + (size_t)t0 * LCH,
+             16u * LCH * nk, mbar);
+  if (GT) bulk_g2s(buf.geo + at, G.geo + t0, 16u * nk, mbar);
 }
 
 // ------------------------------------------------- tensor-core prefilter
@@ -337,6 +343,22 @@ __device__ __forceinline__ void write_row_sums(float *rs, int mode, const KParam
   rs[6] = as;
 }
 
+// The warp's 32 source rows, for lanes that evaluate another lane's row.
+template <int FCH, int LCH>
+struct __align__(16) SrcRows {
+  float4 x[32];                                // position, ||x||
+  float4 rc[32];                               // l, d2 threshold, 1 / (2 l^2), geometric type g0
+  float4 f[32 * (FCH > 0 ? FCH : 1)];
+  float4 l[32 * (LCH > 0 ? LCH : 1)];
+  float g1[32];                                // geometric type g1
+};
+
+// Position of the (n+1)-th set bit of m (n >= 0, m has more than n set bits).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
+  for (int i = 0; i < n; i++) m &= m - 1u;
+  return __ffs(m) - 1;
+}
+
 // Dynamic shared memory of one k_assoc block: per warp two staging buffers, the
 // prefilter tile, the grid descriptor and two mbarriers (16-byte aligned pieces).
 template <int FCH, int LCH, bool GT>
@@ -345,7 +367,8 @@ struct AssocSmem {
   static constexpr size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
   static constexpr size_t kStage = 0;
   static constexpr size_t kMma = align16(kStage + sizeof(StageBuf<FCH, LCH, GT>) * 2 * kWarps);
-  static constexpr size_t kGrid = align16(kMma + sizeof(MmaTile) * kWarps);
+  static constexpr size_t kRows = align16(kMma + sizeof(MmaTile) * kWarps);
+  static constexpr size_t kGrid = align16(kRows + sizeof(SrcRows<FCH, LCH>) * kWarps);
   static constexpr size_t kMbar = align16(kGrid + sizeof(GridDesc) * kWarps);
   static constexpr size_t kBytes = align16(kMbar + sizeof(uint64_t) * 2 * kWarps);
 };
@@ -364,12 +387,14 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
   extern __shared__ __align__(128) unsigned char assoc_smem[];
   Buf(*stage_all)[2] = reinterpret_cast<Buf(*)[2]>(assoc_smem + L::kStage);
   MmaTile *mma_all = reinterpret_cast<MmaTile *>(assoc_smem + L::kMma);
+  SrcRows<FCH, LCH> *rows_all = reinterpret_cast<SrcRows<FCH, LCH> *>(assoc_smem + L::kRows);
   GridDesc *grid_all = reinterpret_cast<GridDesc *>(assoc_smem + L::kGrid);
   uint64_t(*mbar_all)[2] = reinterpret_cast<uint64_t(*)[2]>(assoc_smem + L::kMbar);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   Buf *stage = stage_all[wib];
   MmaTile &mt = mma_all[wib];
+  SrcRows<FCH, LCH> &sr = rows_all[wib];
   uint64_t *mbar = mbar_all[wib];
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= B.total_warps) return;
@@ -390,7 +415,6 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
   const bool valid = s < n;
   const float ell = P->ell;
   const int cap = P->cap;
-  const int mode = P->mode;
   const int F = P->F, C = P->C;
   float4 x = valid ? __ldg(&P->xs[s]) : make_float4(0.f, 0.f, 0.f, 0.f);
   float4 xf[FCH > 0 ? FCH : 1];
@@ -464,32 +488,30 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
     av[15] = 0.f;
     const bool ok = mma_store_vec(av, mt.a, lane);
     use_mma = __all_sync(FULLMASK, ok);
+    // this row's data for the lanes that evaluate its surviving pairs
+    sr.x[lane] = x;
+    sr.rc[lane] = make_float4(rc.l, rc.d2t, rc.inv2l2, xg.x);
+    sr.g1[lane] = xg.y;
+#pragma unroll
+    for (int q = 0; q < (FCH > 0 ? FCH : 1); q++) sr.f[lane * (FCH > 0 ? FCH : 1) + q] = xf[q];
+#pragma unroll
+    for (int q = 0; q < (LCH > 0 ? LCH : 1); q++) sr.l[lane * (LCH > 0 ? LCH : 1) + q] = xl[q];
     __syncwarp();
   }
   int cnt = 0;
-  float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
   const float4 *__restrict__ ycur = P->ycur;
-  const EllRow row{P->A_j + (valid ? s : 0), P->A_v + (valid ? s : 0), (size_t)n};
   const int ov = P->ov;
-  int2 *const ovf_row = P->ovf + (valid ? (size_t)s * ov : 0);
+  const int tile0 = (gw - B.tile_off[p]) * 32;   // source index of lane 0's row
   bool lost = false;
-  // a kept pair enters the row: ELL slot (first cap, with the partial sums) or overflow entry
-  auto keep = [&](float a, const float4 &y) {
-    const int j = __float_as_int(y.w);
-    if (cnt < cap) {
-      row.J(cnt) = j;
-      row.V(cnt) = a;
-      w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
-      w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
-      w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
-      v0 = fmaf(a, y.x - x.x, v0);
-      v1 = fmaf(a, y.y - x.y, v1);
-      v2 = fmaf(a, y.z - x.z, v2);
-      as += a;
-    } else if (cnt - cap < ov) {
-      ovf_row[cnt - cap] = make_int2(j, __float_as_int(a));
+  // kept pair number `slot` of row r enters its ELL slot (first cap) or overflow entry
+  auto put = [&](int r, int slot, int j, float a) {
+    const size_t sidx = (size_t)(tile0 + r);
+    if (slot < cap) {
+      P->A_j[(size_t)slot * n + sidx] = j;
+      P->A_v[(size_t)slot * n + sidx] = a;
+    } else if (slot - cap < ov) {
+      P->ovf[sidx * ov + (slot - cap)] = make_int2(j, __float_as_int(a));
     }
-    cnt++;
   };
   for (int pass = 0; pass < npass && !lost; pass++) {
     int x0, y0, z0, nx, ny, nz;
@@ -503,43 +525,82 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
     } else {
       x0 = ux0; y0 = uy0; z0 = uz0; nx = unx; ny = uny; nz = unz;
     }
+    // bounding box of this pass's query points and their largest search radius
+    float bl0 = qx, bl1 = qy, bl2 = qz, bh0 = qx, bh1 = qy, bh2 = qz, brq = valid ? rc.rq : 0.f;
+    if (per_lane) {
+      bl0 = bh0 = __shfl_sync(FULLMASK, qx, pass); bl1 = bh1 = __shfl_sync(FULLMASK, qy, pass);
+      bl2 = bh2 = __shfl_sync(FULLMASK, qz, pass); brq = __shfl_sync(FULLMASK, brq, pass);
+    } else {
+      bl0 = warp_min(valid ? qx : INFINITY); bl1 = warp_min(valid ? qy : INFINITY); bl2 = warp_min(valid ? qz : INFINITY);
+      bh0 = warp_max(valid ? qx : -INFINITY); bh1 = warp_max(valid ? qy : -INFINITY); bh2 = warp_max(valid ? qz : -INFINITY);
+      brq = warp_max(brq);
+    }
+    const float slack = 1e-3f * G.h;
+    const float prune_r2 = (brq + slack) * (brq + slack);
     const int ncells = nx * ny * nz;
     for (int cb = 0; cb < ncells && !lost; cb += 32) {
       int ci = cb + lane;
       int2 se = make_int2(0, 0);
       if (ci < ncells) {
         int cx = x0 + ci % nx, cy = y0 + (ci / nx) % ny, cz = z0 + ci / (nx * ny);
-        se = grid_lookup(G, cx, cy, cz);
+        // skip cells farther than the largest radius from every query point of the pass
+        bool near = true;
+        if (G.inv_h != 0.f) {
+          const float c0 = fmaf((float)cx, G.h, G.ox), c1 = fmaf((float)cy, G.h, G.oy), c2 = fmaf((float)cz, G.h, G.oz);
+          const float dx = fmaxf(fmaxf(c0 - bh0, bl0 - (c0 + G.h)), 0.f);
+          const float dy = fmaxf(fmaxf(c1 - bh1, bl1 - (c1 + G.h)), 0.f);
+          const float dz = fmaxf(fmaxf(c2 - bh2, bl2 - (c2 + G.h)), 0.f);
+          near = dx * dx + dy * dy + dz * dz <= prune_r2;
+        }
+        if (near) se = grid_lookup(G, cx, cy, cz);
       }
       unsigned mk = __ballot_sync(FULLMASK, se.y > 0);
       if (!mk) continue;
-      // chunk walk over the non-empty cells' segments
-      int b = __ffs(mk) - 1;
-      mk &= mk - 1;
-      int seg_start = __shfl_sync(FULLMASK, se.x, b);
-      int seg_cnt = __shfl_sync(FULLMASK, se.y, b);
-      int off = 0;
-      int cur = 0;
-      if (lane == 0) stage_issue<FCH, LCH, GT>(stage[cur], &mbar[cur], ycur, G, seg_start, min(CH, seg_cnt));
-      while (true) {
-        const int nk = min(CH, seg_cnt - off);
-        // next chunk: rest of this segment, else the next non-empty cell
-        int n_start = seg_start, n_cnt = seg_cnt, n_off = off + CH;
-        bool has_next = true;
-        if (n_off >= seg_cnt) {
-          if (mk) {
-            int b2 = __ffs(mk) - 1;
-            mk &= mk - 1;
-            n_start = __shfl_sync(FULLMASK, se.x, b2);
-            n_cnt = __shfl_sync(FULLMASK, se.y, b2);
-            n_off = 0;
-          } else {
-            has_next = false;
+      // Chunks of up to CH candidates filled from consecutive non-empty cells of this
+      // batch; the warp walks a cursor (cell, offset) in lockstep and lane 0 issues
+      // one bulk copy set per piece.
+      int c_start = 0, c_cnt = 0, c_off = 0;
+      auto fill = [&](int bi) -> int {
+        unsigned m2 = mk;
+        int n2 = c_cnt, o2 = c_off, filled = 0;
+        while (filled < CH) {
+          if (o2 >= n2) {
+            if (!m2) break;
+            const int bb = __ffs(m2) - 1;
+            m2 &= m2 - 1;
+            n2 = __shfl_sync(FULLMASK, se.y, bb);
+            o2 = 0;
           }
+          const int take = min(CH - filled, n2 - o2);
+          filled += take;
+          o2 += take;
         }
-        if (has_next && lane == 0)
-          stage_issue<FCH, LCH, GT>(stage[cur ^ 1], &mbar[cur ^ 1], ycur, G, n_start + n_off,
-                                    min(CH, n_cnt - n_off));
+        if (filled == 0) return 0;
+        if (lane == 0) {
+          fence_proxy_async_smem();   // the lanes' reads of this buffer precede the copies into it
+          mbar_arrive_expect_tx(&mbar[bi], StageRec<FCH, LCH, GT>::kBytes * (uint32_t)filled);
+        }
+        int at = 0;
+        while (at < filled) {
+          if (c_off >= c_cnt) {
+            const int bb = __ffs(mk) - 1;
+            mk &= mk - 1;
+            c_start = __shfl_sync(FULLMASK, se.x, bb);
+            c_cnt = __shfl_sync(FULLMASK, se.y, bb);
+            c_off = 0;
+          }
+          const int take = min(filled - at, c_cnt - c_off);
+          if (lane == 0) stage_piece<FCH, LCH, GT>(stage[bi], &mbar[bi], ycur, G, at, c_start + c_off, take);
+          at += take;
+          c_off += take;
+        }
+        return filled;
+      };
+      int cur = 0;
+      int nk = fill(cur);
+      while (nk > 0) {
+        const int nk_next = fill(cur ^ 1);
+        const bool has_next = nk_next > 0;
         const bool ok = __all_sync(FULLMASK, mbar_wait(&mbar[cur], parity[cur], kWaitLimit));
         parity[cur] ^= 1u;
         if (!ok) {
@@ -580,17 +641,55 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
           uint32_t cand = ok ? mma_filter(mt, lane, K.mma_tau) : 0xFFFFFFFFu;
           cand &= (nk >= 32) ? 0xFFFFFFFFu : ((1u << nk) - 1u);
           if (!me) cand = 0u;
-          // exact evaluation of the surviving pairs, ascending candidate order per row
-          while (__any_sync(FULLMASK, cand != 0u)) {
-            const bool pre = cand != 0u;
-            const int k = pre ? __ffs(cand) - 1 : 0;
-            cand &= cand - 1u;
+          // Exact evaluation of the surviving pairs, 32 at a time: pair number i of the
+          // warp (rows in order, each row's candidates ascending) goes to lane i % 32,
+          // so a row's kept pairs still enter it in ascending candidate order.
+          const int cc = __popc(cand);
+          int incl = cc;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULLMASK, incl, o);
+            if (lane >= o) incl += t;
+          }
+          const int excl = incl - cc;
+          const int total = __shfl_sync(FULLMASK, incl, 31);
+          for (int b0 = 0; b0 < total; b0 += 32) {
+            const int idx = b0 + lane;
+            const bool has = idx < total;
+            int r = 0;   // row of pair idx: the last row whose first pair is at or before idx
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+              const int e = __shfl_sync(FULLMASK, excl, r + st);
+              if (e <= idx) r += st;
+            }
+            const int er = __shfl_sync(FULLMASK, excl, r);
+            const uint32_t mr = __shfl_sync(FULLMASK, cand, r);
+            const int cr = __shfl_sync(FULLMASK, cnt, r);
+            const int k = has ? nth_set_bit(mr, idx - er) : 0;
+            const float4 xr = sr.x[r];
+            const float4 rr = sr.rc[r];
+            float4 xfr[FCH > 0 ? FCH : 1];
+            float4 xlr[LCH > 0 ? LCH : 1];
+#pragma unroll
+            for (int q = 0; q < (FCH > 0 ? FCH : 1); q++) xfr[q] = sr.f[r * (FCH > 0 ? FCH : 1) + q];
+#pragma unroll
+            for (int q = 0; q < (LCH > 0 ? LCH : 1); q++) xlr[q] = sr.l[r * (LCH > 0 ? LCH : 1) + q];
+            const float2 xgr = make_float2(rr.w, sr.g1[r]);
             const float4 y = sb.pos[k];
             float a;
-            bool acc = eval_pair<FCH, LCH, GT>(K, F, C, pre, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y,
-                                               &sb.feat[k * (FCH > 0 ? FCH : 1)], &sb.lab[k * (LCH > 0 ? LCH : 1)],
-                                               &sb.geo[GT ? k : 0], a);
-            if (acc) keep(a, y);
+            const bool acc = eval_pair<FCH, LCH, GT>(K, F, C, has, rr.x, rr.y, rr.z, xr, xfr, xlr, xgr, y,
+                                                     &sb.feat[k * (FCH > 0 ? FCH : 1)],
+                                                     &sb.lab[k * (LCH > 0 ? LCH : 1)], &sb.geo[GT ? k : 0], a);
+            const uint32_t bal = __ballot_sync(FULLMASK, acc);
+            if (acc) {
+              const int lo = max(er - b0, 0);
+              const uint32_t before = bal & ((1u << lane) - 1u) & ~((1u << lo) - 1u);
+              put(r, cr + __popc(before), __float_as_int(y.w), a);
+            }
+            // row owners count their kept pairs of this group
+            const int lo = min(max(excl - b0, 0), 32), hi = min(max(incl - b0, 0), 32);
+            const uint32_t seg = (uint32_t)(((1ull << hi) - 1ull) & ~((1ull << lo) - 1ull));
+            cnt += __popc(bal & seg);
           }
         } else {
           for (int k = 0; k < nk; k++) {
@@ -599,14 +698,11 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
             bool acc = eval_pair<FCH, LCH, GT>(K, F, C, me, rc.l, rc.d2t, rc.inv2l2, x, xf, xl, xg, y,
                                                &sb.feat[k * (FCH > 0 ? FCH : 1)], &sb.lab[k * (LCH > 0 ? LCH : 1)],
                                                &sb.geo[GT ? k : 0], a);
-            if (acc) keep(a, y);
+            if (acc) { put(lane, cnt, __float_as_int(y.w), a); cnt++; }
           }
         }
         __syncwarp();
-        if (!has_next) break;
-        seg_start = n_start;
-        seg_cnt = n_cnt;
-        off = n_off;
+        nk = nk_next;
         cur ^= 1;
       }
     }
@@ -614,8 +710,6 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
   if (valid && !lost) {
     const int kept = cnt < cap ? cnt : cap;
     P->nnz_row[s] = kept;
-    float *rs = P->row_sums + (size_t)s * 8;
-    write_row_sums(rs, mode, K, w0, w1, w2, v0, v1, v2, as);
     if (cnt > cap && cap > 0) {
       // more than cap kept pairs: the row's set is finished by k_select / k_rescan
       if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
@@ -628,11 +722,22 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
 constexpr int kSelMax = 2048;      // ELL + overflow entries one row can hold (cap + ov)
 constexpr int kSelThreads = 128;
 
-// Partial sums of kept pairs of source point x over one warp: per-lane FP32 sums,
-// then a fixed-order warp tree (deterministic).
-struct RowAcc {
+// Row partials of one source row from its final ELL entries, in slot order
+// (thread per row): omega = sum a (x cross y), v = sum a (y - x), sum a.
+// (CvoGPU.cu:2001-2062 computes the same sums from the sparse kernel matrix.)
+__global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= B.total_rows) return;
+  const int p = find_segment(B.row_off, B.npairs, g);
+  const PairDev *P = &B.pairs[p];
+  if (P->done) return;
+  const int s = g - B.row_off[p], n = P->n;
+  const int z = P->nnz_row[s];
+  const float4 x = __ldg(&P->xs[s]);
   float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
-  __device__ __forceinline__ void add(const float4 &x, const float4 &y, float a) {
+  for (int c = 0; c < z; c++) {
+    const float a = P->A_v[(size_t)c * n + s];
+    const float4 y = __ldg(&P->yorig[P->A_j[(size_t)c * n + s]]);
     w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
     w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
     w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
@@ -641,12 +746,8 @@ struct RowAcc {
     v2 = fmaf(a, y.z - x.z, v2);
     as += a;
   }
-  __device__ __forceinline__ void write(float *rs, int mode, const KParams &K, int lane) {
-    w0 = warp_sumf(w0); w1 = warp_sumf(w1); w2 = warp_sumf(w2);
-    v0 = warp_sumf(v0); v1 = warp_sumf(v1); v2 = warp_sumf(v2); as = warp_sumf(as);
-    if (lane == 0) write_row_sums(rs, mode, K, w0, w1, w2, v0, v1, v2, as);
-  }
-};
+  write_row_sums(P->row_sums + (size_t)s * 8, P->mode, K, w0, w1, w2, v0, v1, v2, as);
+}
 
 // One warp per listed row with cap < count <= cap + ov: the row's cap ELL entries
 // and its overflow entries hold every kept pair; the cap-th smallest target index
@@ -674,8 +775,6 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       for (int t = lane; t < E; t += 32) c += jb[t] < tv ? 1 : 0;
       if (warp_sumi(c) < cap) r = tv;
     }
-    const float4 x = P->xs[s];
-    RowAcc acc;
     int base = 0;
     for (int t0 = 0; t0 < E; t0 += 32) {
       const int t = t0 + lane;
@@ -692,11 +791,9 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
         const int c = base + __popc(bal & ((1u << lane) - 1u));
         P->A_j[(size_t)c * n + s] = j;
         P->A_v[(size_t)c * n + s] = a;
-        acc.add(x, __ldg(&P->yorig[j]), a);
       }
       base += __popc(bal);
     }
-    acc.write(P->row_sums + (size_t)s * 8, P->mode, K, lane);
     __syncwarp();
   }
 }
@@ -725,7 +822,6 @@ __global__ void __launch_bounds__(kSelThreads) k_rescan(BatchDev B, KParams K) {
     const float2 xg = GT ? __ldg(&P->xg[s]) : make_float2(0.f, 0.f);
     const float Tn = fabsf(P->T[0]) + fabsf(P->T[1]) + fabsf(P->T[2]);
     const RowConst rc = row_const(K, P->ell, x.w, Tn);
-    RowAcc acc;
     int taken = 0;
     for (int j0 = 0; j0 < m && taken < cap; j0 += 32) {
       const int j = j0 + lane;
@@ -744,12 +840,10 @@ __global__ void __launch_bounds__(kSelThreads) k_rescan(BatchDev B, KParams K) {
         if (c < cap) {
           P->A_j[(size_t)c * n + s] = j;
           P->A_v[(size_t)c * n + s] = a;
-          acc.add(x, y, a);
         }
       }
       taken += __popc(bal);
     }
-    acc.write(P->row_sums + (size_t)s * 8, P->mode, K, lane);
   }
 }
 
