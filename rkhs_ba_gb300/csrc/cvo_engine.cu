@@ -12,6 +12,7 @@
 #include <chrono>
 #include "cvo_internal.h"
 #include "cvo_kernels.cuh"
+#include "cvo_assoc_cta.cuh"
 #include "cvo_lie.cuh"
 
 namespace cvo_gb {
@@ -306,9 +307,9 @@ using AssocFn = void (*)(BatchDev, KParams);
 // the storage strides of the clouds.
 template <int FC, int LC, bool G>
 static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem) {
-  a = k_assoc<FC, LC, G>;
+  a = k_assoc_cta<FC, LC, G>;
   rs = k_rescan<FC, LC, G>;
-  smem = AssocSmem<FC, LC, G>::kBytes;
+  smem = CtaSmem<FC, LC, G>::kBytes;
   // opt in above the 48 KB default once per device (setting it twice is harmless)
   static unsigned long long set_mask = 0;
   int dev = 0;
@@ -509,15 +510,16 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
   int max_part_blocks = 0;
-  // overflow entries per row: up to 3 cap, within kSelMax, and at most 4 GB for the batch
+  // overflow entries per row: up to kSelMax - cap, and at most 8 GB for the batch
   long long rows_all = 0;
   for (int p = 0; p < np; p++) rows_all += srcs[p]->n;
-  int ov = std::max(0, std::min(3 * capmax, kSelMax - capmax));
-  if (rows_all > 0) ov = (int)std::min<long long>(ov, (4ll << 30) / (8ll * rows_all));
+  int ov = std::max(0, kSelMax - capmax);
+  if (rows_all > 0) ov = (int)std::min<long long>(ov, (8ll << 30) / (8ll * rows_all));
   bh->ov = ov;
   for (int p = 0; p < np; p++) {
     int n = srcs[p]->n, m = tgts[p]->n;
-    bh->tile_off[p + 1] = bh->tile_off[p] + (n + 31) / 32;
+    // tiles per pair padded to whole association blocks (kCtaWarps tiles of one pair)
+    bh->tile_off[p + 1] = bh->tile_off[p] + ((n + 32 * kCtaWarps - 1) / (32 * kCtaWarps)) * kCtaWarps;
     bh->row_off[p + 1] = bh->row_off[p] + n;
     bh->tgt_off[p + 1] = bh->tgt_off[p] + m;
     int rb = (n + kReduceRows - 1) / kReduceRows, sb = (n + kStepThreads - 1) / kStepThreads;

@@ -63,25 +63,20 @@ __global__ void k_morton(const float4 *pos, int n, float ox, float oy, float oz,
   vals[i] = i;
 }
 
-// Bounding-box diagonal of each 32-point tile (one warp per tile).
+// Bounding-box diagonal of each block of 128 consecutive tile-order points (one
+// thread per block of points).
 __global__ void k_tile_extent(const float4 *spos, int n, float *ext) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tile = g >> 5, lane = g & 31;
-  const int tiles = (n + 31) / 32;
+  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tiles = (n + 127) / 128;
   if (tile >= tiles) return;
-  const int s = tile * 32 + lane;
-  float4 p = s < n ? spos[s] : spos[tile * 32];
-  float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z};
-  for (int k = 0; k < 3; k++) {
-    for (int o = 16; o > 0; o >>= 1) {
-      lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
-      hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
-    }
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int s = tile * 128; s < min(n, tile * 128 + 128); s++) {
+    const float4 p = spos[s];
+    lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+    hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
   }
-  if (lane == 0) {
-    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
-    ext[tile] = sqrtf(dx * dx + dy * dy + dz * dz);
-  }
+  const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+  ext[tile] = sqrtf(dx * dx + dy * dy + dz * dz);
 }
 
 __global__ void k_gather_source(const int *perm, int n, const float4 *pos, const float *feat, int FP, const float *lab,
@@ -228,10 +223,10 @@ int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
   k_gather_source<<<(n + 255) / 256, 256, 0, h->stream>>>(d->sperm, n, d->pos, d->feat, d->FP, d->lab, d->CP, d->geo,
                                                          d->spos, d->sfeat, d->slab, d->sgeo);
   h->launches++;
-  // mean bounding-box diagonal of the 32-point source tiles (sizes the grid cells)
-  const int tiles = (n + 31) / 32;
+  // mean bounding-box diagonal of the 128-point source blocks (sizes the grid cells)
+  const int tiles = (n + 127) / 128;
   float *ext_d = reinterpret_cast<float *>(keys);
-  k_tile_extent<<<(tiles * 32 + 255) / 256, 256, 0, h->stream>>>(d->spos, n, ext_d);
+  k_tile_extent<<<(tiles + 127) / 128, 128, 0, h->stream>>>(d->spos, n, ext_d);
   h->launches++;
   std::vector<float> ext_h(tiles);
   CVO_CUDA_TRY(h, cudaMemcpyAsync(ext_h.data(), ext_d, sizeof(float) * tiles, cudaMemcpyDeviceToHost, h->stream));

@@ -49,7 +49,7 @@ struct DevCloud {
   bool has_geo = false;
   float bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
   float max_norm = 0.f;
-  float tile_ext = 0.f;          // mean bounding-box diagonal of the 32-point source tiles
+  float tile_ext = 0.f;          // mean bounding-box diagonal of 128 consecutive tile-order points
   // original order
   float4 *pos = nullptr;
   float *feat = nullptr;

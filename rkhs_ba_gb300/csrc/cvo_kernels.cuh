@@ -241,9 +241,10 @@ __device__ __forceinline__ float f4_at(const float4 &v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// Splits v into f16 hi + lo and stores entry `idx` of the 4 planes; returns false
+// Splits v into f16 hi + lo and stores entry `idx` of the 4 planes (plane p at
+// dst + p * stride); returns false
 // if a component is outside the f16-safe range (or not finite).
-__device__ __forceinline__ bool mma_store_vec(const float (&v)[16], uint4 (*dst)[32], int idx) {
+__device__ __forceinline__ bool mma_store_vec(const float (&v)[16], uint4 *dst, int stride, int idx) {
   uint32_t hw[8], lw[8];
   bool ok = true;
 #pragma unroll
@@ -255,10 +256,10 @@ __device__ __forceinline__ bool mma_store_vec(const float (&v)[16], uint4 (*dst)
     hw[i] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
     lw[i] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
   }
-  dst[0][idx] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-  dst[1][idx] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-  dst[2][idx] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-  dst[3][idx] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+  dst[idx] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  dst[stride + idx] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+  dst[2 * stride + idx] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  dst[3 * stride + idx] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
   return ok;
 }
 
@@ -275,60 +276,6 @@ __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4],
       "{%0, %1, %2, %3};\n"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// A fragments (rows 16m..16m+15) of plane pair `base` (0 = hi, 2 = lo).
-__device__ __forceinline__ void mma_load_a(const MmaTile &T, int base, int m, int lane, uint32_t (&a)[4]) {
-  const int mi = lane >> 3, r8 = lane & 7;
-  ldsm_x4(&T.a[base + (mi >> 1)][16 * m + 8 * (mi & 1) + r8], a[0], a[1], a[2], a[3]);
-}
-
-// B fragments of candidate groups 2j and 2j+1 (candidates 16j..16j+15).
-__device__ __forceinline__ void mma_load_b(const MmaTile &T, int base, int j, int lane, uint32_t (&b)[4]) {
-  const int mi = lane >> 3, r8 = lane & 7;
-  ldsm_x4(&T.b[base + (mi & 1)][16 * j + 8 * (mi >> 1) + r8], b[0], b[1], b[2], b[3]);
-}
-
-// u-tile of the warp's 32 rows against the 32 staged candidates; returns, for the
-// lane's own row, the bit mask of candidates with u < tau.  All lanes call it.
-__device__ __forceinline__ uint32_t mma_filter(const MmaTile &T, int lane, float tau) {
-  uint32_t word = 0;   // byte (2m + h), bit (2n + jj): row 16m + 8h + lane/4, column 8n + 2(lane%4) + jj
-#pragma unroll
-  for (int j = 0; j < 2; j++) {
-    uint32_t bh[4], bl[4];
-    mma_load_b(T, 0, j, lane, bh);
-    mma_load_b(T, 2, j, lane, bl);
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-      uint32_t ah[4], al[4];
-      mma_load_a(T, 0, m, lane, ah);
-      mma_load_a(T, 2, m, lane, al);
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        const int n = 2 * j + q;
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        mma_16816(d, ah, bh[2 * q], bh[2 * q + 1]);
-        mma_16816(d, ah, bl[2 * q], bl[2 * q + 1]);
-        mma_16816(d, al, bh[2 * q], bh[2 * q + 1]);
-        word |= (d[0] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n);
-        word |= (d[1] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n + 1);
-        word |= (d[2] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n);
-        word |= (d[3] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n + 1);
-      }
-    }
-  }
-  // gather the lane's row: held by lanes 4 (row % 8) + t, t = 0..3
-  const int sh = 8 * (2 * (lane >> 4) + ((lane >> 3) & 1));
-  const int src0 = 4 * (lane & 7);
-  uint32_t mask = 0;
-#pragma unroll
-  for (int t = 0; t < 4; t++) {
-    const uint32_t w = __shfl_sync(FULLMASK, word, src0 + t);
-    const uint32_t b = (w >> sh) & 0xFFu;
-    const uint32_t s = (b & 0x3u) | ((b & 0xCu) << 6) | ((b & 0x30u) << 12) | ((b & 0xC0u) << 18);
-    mask |= s << (2 * t);
-  }
-  return mask;
 }
 
 // Row partials as k_reduce reads them: omega / c, v / d (align mode only), sum of a.
@@ -359,6 +306,16 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
   return __ffs(m) - 1;
 }
 
+// Kept count of a finished row; a row with more than cap kept pairs is listed for
+// k_select (its overflow entries hold them all) or k_rescan.
+__device__ __forceinline__ void finish_row(const BatchDev &B, PairDev *P, int p, int s, int cnt, int cap, int ov) {
+  P->nnz_row[s] = cnt < cap ? cnt : cap;
+  if (cnt > cap && cap > 0) {
+    if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
+    else B.scan_list[atomicAdd(B.scan_count, 1)] = make_int4(p, s, cnt, 0);
+  }
+}
+
 // Dynamic shared memory of one k_assoc block: per warp two staging buffers, the
 // prefilter tile, the grid descriptor and two mbarriers (16-byte aligned pieces).
 template <int FCH, int LCH, bool GT>
@@ -373,6 +330,169 @@ struct AssocSmem {
   static constexpr size_t kBytes = align16(kMbar + sizeof(uint64_t) * 2 * kWarps);
 };
 
+// Plane p of a row/candidate block: entry i at base[p * stride + i] (16 B = 8 halves).
+// A fragments (rows 16m..16m+15) of plane pair `hl` (0 = hi, 2 = lo).
+__device__ __forceinline__ void mma_load_a(const uint4 *a, int stride, int hl, int m, int lane, uint32_t (&r)[4]) {
+  const int mi = lane >> 3, r8 = lane & 7;
+  ldsm_x4(&a[(hl + (mi >> 1)) * stride + 16 * m + 8 * (mi & 1) + r8], r[0], r[1], r[2], r[3]);
+}
+
+// B fragments of candidate groups 2j and 2j+1 (candidates 16j..16j+15).
+__device__ __forceinline__ void mma_load_b(const uint4 *b, int stride, int hl, int j, int lane, uint32_t (&r)[4]) {
+  const int mi = lane >> 3, r8 = lane & 7;
+  ldsm_x4(&b[(hl + (mi & 1)) * stride + 16 * j + 8 * (mi >> 1) + r8], r[0], r[1], r[2], r[3]);
+}
+
+// u-tile of 32 rows (planes at a, stride as) against 32 candidates (planes at b,
+// stride bs); returns, for the lane's own row, the bit mask of candidates with
+// u < tau.  All lanes call it.
+__device__ __forceinline__ uint32_t mma_filter(const uint4 *a, int as, const uint4 *b, int bs, int lane, float tau) {
+  uint32_t word = 0;   // byte (2m + h), bit (2n + jj): row 16m + 8h + lane/4, column 8n + 2(lane%4) + jj
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    uint32_t bh[4], bl[4];
+    mma_load_b(b, bs, 0, j, lane, bh);
+    mma_load_b(b, bs, 2, j, lane, bl);
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      uint32_t ah[4], al[4];
+      mma_load_a(a, as, 0, m, lane, ah);
+      mma_load_a(a, as, 2, m, lane, al);
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int n = 2 * j + q;
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_16816(d, ah, bh[2 * q], bh[2 * q + 1]);
+        mma_16816(d, ah, bl[2 * q], bl[2 * q + 1]);
+        mma_16816(d, al, bh[2 * q], bh[2 * q + 1]);
+        word |= (d[0] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n);
+        word |= (d[1] < tau ? 1u : 0u) << (8 * (2 * m) + 2 * n + 1);
+        word |= (d[2] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n);
+        word |= (d[3] < tau ? 1u : 0u) << (8 * (2 * m + 1) + 2 * n + 1);
+      }
+    }
+  }
+  // gather the lane's row: held by lanes 4 (row % 8) + t, t = 0..3
+  const int sh = 8 * (2 * (lane >> 4) + ((lane >> 3) & 1));
+  const int src0 = 4 * (lane & 7);
+  uint32_t mask = 0;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const uint32_t w = __shfl_sync(FULLMASK, word, src0 + t);
+    const uint32_t bb = (w >> sh) & 0xFFu;
+    const uint32_t sp = (bb & 0x3u) | ((bb & 0xCu) << 6) | ((bb & 0x30u) << 12) | ((bb & 0xC0u) << 18);
+    mask |= sp << (2 * t);
+  }
+  return mask;
+}
+
+// Filter vector of a source row (A) or a candidate (B), relative to the centre p.
+template <int FCH>
+__device__ __forceinline__ void mma_row_vec(float (&av)[16], bool valid, const float4 &x, const float4 (&xf)[FCH > 0 ? FCH : 1],
+                                            int F, float g, float cw, float px, float py, float pz) {
+  const float tx = x.x - px, ty = x.y - py, tz = x.z - pz;
+  g = valid ? g : 0.f;
+  av[0] = -2.f * g * tx; av[1] = -2.f * g * ty; av[2] = -2.f * g * tz;
+  float xc2 = 0.f;
+#pragma unroll
+  for (int f = 0; f < 8; f++) {
+    float xv = 0.f;
+    if (FCH > 0 && (f >> 2) < FCH && f < F) xv = f4_at(xf[(f >> 2) < FCH ? (f >> 2) : 0], f & 3);
+    av[3 + f] = valid ? -2.f * cw * xv : 0.f;
+    xc2 += xv * xv;
+  }
+  av[11] = g;
+  av[12] = valid ? cw : 0.f;
+  av[13] = valid ? g * (tx * tx + ty * ty + tz * tz) + cw * xc2 : 0.f;
+  float na = 0.f;
+#pragma unroll
+  for (int k = 0; k < 14; k++) na += av[k] * av[k];
+  av[14] = -kMmaKappa * sqrtf(na);
+  av[15] = 0.f;
+}
+
+template <int FCH>
+__device__ __forceinline__ void mma_cand_vec(float (&bv)[16], bool has, const float4 &y, const float4 *yf, int F,
+                                             float px, float py, float pz) {
+#pragma unroll
+  for (int q = 0; q < 16; q++) bv[q] = 0.f;
+  if (!has) return;
+  bv[0] = y.x - px; bv[1] = y.y - py; bv[2] = y.z - pz;
+  float yc2 = 0.f;
+#pragma unroll
+  for (int f = 0; f < 8; f++) {
+    float yv = 0.f;
+    if (FCH > 0 && (f >> 2) < FCH && f < F) yv = f4_at(yf[(f >> 2) < FCH ? (f >> 2) : 0], f & 3);
+    bv[3 + f] = yv;
+    yc2 += yv * yv;
+  }
+  bv[11] = bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2];
+  bv[12] = yc2;
+  bv[13] = 1.f;
+  float nb = 0.f;
+#pragma unroll
+  for (int q = 0; q < 14; q++) nb += bv[q] * bv[q];
+  bv[14] = sqrtf(nb);
+}
+
+// Exact evaluation of the surviving pairs of one candidate group, 32 at a time:
+// pair number i of the warp (rows in order, each row's candidates ascending) goes
+// to lane i % 32, so a row's kept pairs still enter it in ascending candidate
+// order.  `cand` is the lane's own row mask, `cnt` its kept count (updated);
+// put(r, slot, j, a) stores kept pair number `slot` of row r.
+template <int FCH, int LCH, bool GT, class Put>
+__device__ __forceinline__ void eval_survivors(const KParams &K, int F, int C, int lane, uint32_t cand, int &cnt,
+                                               const SrcRows<FCH, LCH> &sr, const float4 *cpos, const float4 *cfeat,
+                                               const float4 *clab, const float4 *cgeo, Put put) {
+  const int cc = __popc(cand);
+  int incl = cc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int excl = incl - cc;
+  const int total = __shfl_sync(FULLMASK, incl, 31);
+  for (int b0 = 0; b0 < total; b0 += 32) {
+    const int idx = b0 + lane;
+    const bool has = idx < total;
+    int r = 0;   // row of pair idx: the last row whose first pair is at or before idx
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+      const int e = __shfl_sync(FULLMASK, excl, r + st);
+      if (e <= idx) r += st;
+    }
+    const int er = __shfl_sync(FULLMASK, excl, r);
+    const uint32_t mr = __shfl_sync(FULLMASK, cand, r);
+    const int cr = __shfl_sync(FULLMASK, cnt, r);
+    const int k = has ? nth_set_bit(mr, idx - er) : 0;
+    const float4 xr = sr.x[r];
+    const float4 rr = sr.rc[r];
+    float4 xfr[FCH > 0 ? FCH : 1];
+    float4 xlr[LCH > 0 ? LCH : 1];
+#pragma unroll
+    for (int q = 0; q < (FCH > 0 ? FCH : 1); q++) xfr[q] = sr.f[r * (FCH > 0 ? FCH : 1) + q];
+#pragma unroll
+    for (int q = 0; q < (LCH > 0 ? LCH : 1); q++) xlr[q] = sr.l[r * (LCH > 0 ? LCH : 1) + q];
+    const float2 xgr = make_float2(rr.w, sr.g1[r]);
+    const float4 y = cpos[k];
+    float a;
+    const bool acc = eval_pair<FCH, LCH, GT>(K, F, C, has, rr.x, rr.y, rr.z, xr, xfr, xlr, xgr, y,
+                                             &cfeat[k * (FCH > 0 ? FCH : 1)], &clab[k * (LCH > 0 ? LCH : 1)],
+                                             &cgeo[GT ? k : 0], a);
+    const uint32_t bal = __ballot_sync(FULLMASK, acc);
+    if (acc) {
+      const int lo = max(er - b0, 0);
+      const uint32_t before = bal & ((1u << lane) - 1u) & ~((1u << lo) - 1u);
+      put(r, cr + __popc(before), __float_as_int(y.w), a);
+    }
+    // row owners count their kept pairs of this group
+    const int lo = min(max(excl - b0, 0), 32), hi = min(max(incl - b0, 0), 32);
+    const uint32_t seg = (uint32_t)(((1ull << hi) - 1ull) & ~((1ull << lo) - 1ull));
+    cnt += __popc(bal & seg);
+  }
+}
+
 // ------------------------------------------------------------ association
 // One warp per tile of 32 spatially adjacent source points (Morton order).  The
 // warp scans the grid cells overlapping the union of its lanes' query boxes;
@@ -380,11 +500,10 @@ struct AssocSmem {
 // every lane against its own source point.  Chunks are double-buffered: the copy
 // of chunk k+1 is in flight while the lanes test chunk k.
 template <int FCH, int LCH, bool GT>
-__global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) {
+__device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, int gw, unsigned char *assoc_smem) {
   using Buf = StageBuf<FCH, LCH, GT>;
   using L = AssocSmem<FCH, LCH, GT>;
   constexpr int CH = Buf::CH;
-  extern __shared__ __align__(128) unsigned char assoc_smem[];
   Buf(*stage_all)[2] = reinterpret_cast<Buf(*)[2]>(assoc_smem + L::kStage);
   MmaTile *mma_all = reinterpret_cast<MmaTile *>(assoc_smem + L::kMma);
   SrcRows<FCH, LCH> *rows_all = reinterpret_cast<SrcRows<FCH, LCH> *>(assoc_smem + L::kRows);
@@ -396,7 +515,6 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
   MmaTile &mt = mma_all[wib];
   SrcRows<FCH, LCH> &sr = rows_all[wib];
   uint64_t *mbar = mbar_all[wib];
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= B.total_warps) return;
   const int p = find_segment(B.tile_off, B.npairs, gw);
   PairDev *P = &B.pairs[p];
@@ -467,26 +585,8 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
     pcy = warp_sumf(valid ? x.y : 0.f) * inv;
     pcz = warp_sumf(valid ? x.z : 0.f) * inv;
     float av[16];
-    const float tx = x.x - pcx, ty = x.y - pcy, tz = x.z - pcz;
-    const float g = valid ? rc.inv2l2 : 0.f;
-    av[0] = -2.f * g * tx; av[1] = -2.f * g * ty; av[2] = -2.f * g * tz;
-    float xc2 = 0.f;
-#pragma unroll
-    for (int f = 0; f < 8; f++) {
-      float xv = 0.f;
-      if (FCH > 0 && (f >> 2) < FCH && f < F) xv = f4_at(xf[(f >> 2) < FCH ? (f >> 2) : 0], f & 3);
-      av[3 + f] = valid ? -2.f * cw * xv : 0.f;
-      xc2 += xv * xv;
-    }
-    av[11] = g;
-    av[12] = valid ? cw : 0.f;
-    av[13] = valid ? g * (tx * tx + ty * ty + tz * tz) + cw * xc2 : 0.f;
-    float na = 0.f;
-#pragma unroll
-    for (int k = 0; k < 14; k++) na += av[k] * av[k];
-    av[14] = -kMmaKappa * sqrtf(na);
-    av[15] = 0.f;
-    const bool ok = mma_store_vec(av, mt.a, lane);
+    mma_row_vec<FCH>(av, valid, x, xf, F, rc.inv2l2, cw, pcx, pcy, pcz);
+    const bool ok = mma_store_vec(av, &mt.a[0][0], 32, lane);
     use_mma = __all_sync(FULLMASK, ok);
     // this row's data for the lanes that evaluate its surviving pairs
     sr.x[lane] = x;
@@ -614,83 +714,13 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
         if (use_mma) {
           // candidate vectors of this chunk (lane k builds candidate k; empty slots are zero)
           float bv[16];
-#pragma unroll
-          for (int q = 0; q < 16; q++) bv[q] = 0.f;
-          if (lane < nk) {
-            const float4 y = sb.pos[lane];
-            bv[0] = y.x - pcx; bv[1] = y.y - pcy; bv[2] = y.z - pcz;
-            float yc2 = 0.f;
-#pragma unroll
-            for (int f = 0; f < 8; f++) {
-              float yv = 0.f;
-              if (FCH > 0 && (f >> 2) < FCH && f < F)
-                yv = f4_at(sb.feat[lane * (FCH > 0 ? FCH : 1) + ((f >> 2) < FCH ? (f >> 2) : 0)], f & 3);
-              bv[3 + f] = yv;
-              yc2 += yv * yv;
-            }
-            bv[11] = bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2];
-            bv[12] = yc2;
-            bv[13] = 1.f;
-            float nb = 0.f;
-#pragma unroll
-            for (int q = 0; q < 14; q++) nb += bv[q] * bv[q];
-            bv[14] = sqrtf(nb);
-          }
-          const bool ok = __all_sync(FULLMASK, mma_store_vec(bv, mt.b, lane));
+          mma_cand_vec<FCH>(bv, lane < nk, sb.pos[lane], &sb.feat[lane * (FCH > 0 ? FCH : 1)], F, pcx, pcy, pcz);
+          const bool ok = __all_sync(FULLMASK, mma_store_vec(bv, &mt.b[0][0], 32, lane));
           __syncwarp();
-          uint32_t cand = ok ? mma_filter(mt, lane, K.mma_tau) : 0xFFFFFFFFu;
+          uint32_t cand = ok ? mma_filter(&mt.a[0][0], 32, &mt.b[0][0], 32, lane, K.mma_tau) : 0xFFFFFFFFu;
           cand &= (nk >= 32) ? 0xFFFFFFFFu : ((1u << nk) - 1u);
           if (!me) cand = 0u;
-          // Exact evaluation of the surviving pairs, 32 at a time: pair number i of the
-          // warp (rows in order, each row's candidates ascending) goes to lane i % 32,
-          // so a row's kept pairs still enter it in ascending candidate order.
-          const int cc = __popc(cand);
-          int incl = cc;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(FULLMASK, incl, o);
-            if (lane >= o) incl += t;
-          }
-          const int excl = incl - cc;
-          const int total = __shfl_sync(FULLMASK, incl, 31);
-          for (int b0 = 0; b0 < total; b0 += 32) {
-            const int idx = b0 + lane;
-            const bool has = idx < total;
-            int r = 0;   // row of pair idx: the last row whose first pair is at or before idx
-#pragma unroll
-            for (int st = 16; st > 0; st >>= 1) {
-              const int e = __shfl_sync(FULLMASK, excl, r + st);
-              if (e <= idx) r += st;
-            }
-            const int er = __shfl_sync(FULLMASK, excl, r);
-            const uint32_t mr = __shfl_sync(FULLMASK, cand, r);
-            const int cr = __shfl_sync(FULLMASK, cnt, r);
-            const int k = has ? nth_set_bit(mr, idx - er) : 0;
-            const float4 xr = sr.x[r];
-            const float4 rr = sr.rc[r];
-            float4 xfr[FCH > 0 ? FCH : 1];
-            float4 xlr[LCH > 0 ? LCH : 1];
-#pragma unroll
-            for (int q = 0; q < (FCH > 0 ? FCH : 1); q++) xfr[q] = sr.f[r * (FCH > 0 ? FCH : 1) + q];
-#pragma unroll
-            for (int q = 0; q < (LCH > 0 ? LCH : 1); q++) xlr[q] = sr.l[r * (LCH > 0 ? LCH : 1) + q];
-            const float2 xgr = make_float2(rr.w, sr.g1[r]);
-            const float4 y = sb.pos[k];
-            float a;
-            const bool acc = eval_pair<FCH, LCH, GT>(K, F, C, has, rr.x, rr.y, rr.z, xr, xfr, xlr, xgr, y,
-                                                     &sb.feat[k * (FCH > 0 ? FCH : 1)],
-                                                     &sb.lab[k * (LCH > 0 ? LCH : 1)], &sb.geo[GT ? k : 0], a);
-            const uint32_t bal = __ballot_sync(FULLMASK, acc);
-            if (acc) {
-              const int lo = max(er - b0, 0);
-              const uint32_t before = bal & ((1u << lane) - 1u) & ~((1u << lo) - 1u);
-              put(r, cr + __popc(before), __float_as_int(y.w), a);
-            }
-            // row owners count their kept pairs of this group
-            const int lo = min(max(excl - b0, 0), 32), hi = min(max(incl - b0, 0), 32);
-            const uint32_t seg = (uint32_t)(((1ull << hi) - 1ull) & ~((1ull << lo) - 1ull));
-            cnt += __popc(bal & seg);
-          }
+          eval_survivors<FCH, LCH, GT>(K, F, C, lane, cand, cnt, sr, sb.pos, sb.feat, sb.lab, sb.geo, put);
         } else {
           for (int k = 0; k < nk; k++) {
             const float4 y = sb.pos[k];
@@ -707,19 +737,18 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
       }
     }
   }
-  if (valid && !lost) {
-    const int kept = cnt < cap ? cnt : cap;
-    P->nnz_row[s] = kept;
-    if (cnt > cap && cap > 0) {
-      // more than cap kept pairs: the row's set is finished by k_select / k_rescan
-      if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
-      else B.scan_list[atomicAdd(B.scan_count, 1)] = make_int4(p, s, cnt, 0);
-    }
-  }
+  if (valid && !lost) finish_row(B, P, p, s, cnt, cap, ov);
+}
+
+template <int FCH, int LCH, bool GT>
+__global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) {
+  extern __shared__ __align__(128) unsigned char assoc_smem[];
+  assoc_warp<FCH, LCH, GT>(B, K, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, assoc_smem);
 }
 
 // ------------------------------------------------------------ selection
-constexpr int kSelMax = 2048;      // ELL + overflow entries one row can hold (cap + ov)
+constexpr int kSelMax = 4096;      // ELL + overflow entries one row can hold (cap + ov)
+constexpr int kSelStage = 2048;    // rows up to this many entries are selected from shared memory
 constexpr int kSelThreads = 128;
 
 // Row partials of one source row from its final ELL entries, in slot order
@@ -750,13 +779,17 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
 }
 
 // One warp per listed row with cap < count <= cap + ov: the row's cap ELL entries
-// and its overflow entries hold every kept pair; the cap-th smallest target index
-// is found by a bitwise search of counts, and the entries with index up to it
-// (exactly cap, indices are distinct) are compacted into the ELL slots in entry order.
+// and its overflow entries hold every kept pair.  A three-digit radix select
+// (8 + 8 + 6 bits of the 22-bit target index, warp-private histograms in shared
+// memory) finds the cap-th smallest index r; the entries with index <= r (exactly
+// cap, indices are distinct) are compacted into the ELL slots in entry order.
+// Indices are staged in shared memory when the row fits (kSelStage entries).
 __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
-  __shared__ int jbuf_all[kSelThreads / 32][kSelMax];
+  __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
+  __shared__ int hist_all[kSelThreads / 32][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *jb = jbuf_all[w];
+  int *hist = hist_all[w];
   const int count = *B.sel_count;
   const int nwarps = gridDim.x * (kSelThreads / 32);
   for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
@@ -765,16 +798,50 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     const int s = it.y, n = P->n, cap = P->cap, ov = P->ov;
     const int E = cap + min(it.z - cap, ov);
     const int2 *ovf = P->ovf + (size_t)s * ov;
-    for (int t = lane; t < E; t += 32) jb[t] = t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
-    __syncwarp();
-    // r = largest value with #{j < r} < cap, i.e. the cap-th smallest index
-    int r = 0;
-    for (int b = kMaxTargetBits - 1; b >= 0; b--) {
-      const int tv = r | (1 << b);
-      int c = 0;
-      for (int t = lane; t < E; t += 32) c += jb[t] < tv ? 1 : 0;
-      if (warp_sumi(c) < cap) r = tv;
+    const bool staged = E <= kSelStage;
+    auto entry = [&](int t) -> int {
+      if (staged) return jb[t];
+      return t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
+    };
+    if (staged) {
+      for (int t = lane; t < E; t += 32) jb[t] = t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
     }
+    __syncwarp();
+    int prefix = 0, target = cap;
+    const int shifts[3] = {14, 6, 0}, widths[3] = {8, 8, 6};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const int sh = shifts[d], wd = widths[d], hs = sh + wd;
+      for (int b = lane; b < 256; b += 32) hist[b] = 0;
+      __syncwarp();
+      for (int t = lane; t < E; t += 32) {
+        const int j = entry(t);
+        if ((j >> hs) == (prefix >> hs)) atomicAdd(&hist[(j >> sh) & ((1 << wd) - 1)], 1);
+      }
+      __syncwarp();
+      int loc = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) loc += hist[lane * 8 + i];
+      int incl = loc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULLMASK, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int L = __ffs(__ballot_sync(FULLMASK, incl >= target)) - 1;
+      int run = __shfl_sync(FULLMASK, incl - loc, L);
+      int bin = L * 8;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int hb = hist[L * 8 + i];
+        if (run + hb >= target) { bin = L * 8 + i; break; }
+        run += hb;
+      }
+      prefix |= bin << sh;
+      target -= run;
+      __syncwarp();
+    }
+    const int r = prefix;   // the cap-th smallest kept index
     int base = 0;
     for (int t0 = 0; t0 < E; t0 += 32) {
       const int t = t0 + lane;
@@ -782,7 +849,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       float a = 0.f;
       bool k = false;
       if (t < E) {
-        j = jb[t];
+        j = entry(t);
         k = j <= r;
         a = t < cap ? P->A_v[(size_t)t * n + s] : __int_as_float(ovf[t - cap].y);
       }
