@@ -203,9 +203,8 @@ __global__ void __launch_bounds__(kCtaRows) k_assoc_cta(BatchDev B, KParams K) {
     if (slot < cap) {
       P->A_j[(size_t)slot * n + sidx] = j;
       P->A_v[(size_t)slot * n + sidx] = a;
-    } else if (slot - cap < ov) {
-      P->ovf[sidx * ov + (slot - cap)] = make_int2(j, __float_as_int(a));
     }
+    if (slot < ov) P->ovf[sidx * ov + slot] = make_int2(j, __float_as_int(a));
   };
   // cells farther than the largest radius from every query point are skipped
   const float slack = 1e-3f * G.h;

@@ -510,10 +510,10 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
   int max_part_blocks = 0;
-  // overflow entries per row: up to kSelMax - cap, and at most 8 GB for the batch
+  // row-list entries per row (every kept pair, row-major): up to kSelMax, at most 8 GB for the batch
   long long rows_all = 0;
   for (int p = 0; p < np; p++) rows_all += srcs[p]->n;
-  int ov = std::max(0, kSelMax - capmax);
+  int ov = kSelMax;
   if (rows_all > 0) ov = (int)std::min<long long>(ov, (8ll << 30) / (8ll * rows_all));
   bh->ov = ov;
   for (int p = 0; p < np; p++) {
@@ -530,7 +530,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     add(sizeof(float4) * m);                                     // yorig
     add(sizeof(int) * (size_t)n * capmax);                       // ELL (every mode: the row selection uses it)
     add(sizeof(float) * (size_t)n * capmax);
-    add(sizeof(int2) * (size_t)n * ov);                          // overflow entries
+    add(sizeof(int2) * (size_t)n * ov);                          // row lists
     add(sizeof(int) * n);                                        // nnz_row
     add(sizeof(float) * 8 * (size_t)n);                          // row_sums
     add(sizeof(double) * kPartStride * (size_t)std::max(rb, sb)); // partials

@@ -99,8 +99,8 @@ struct PairDev {
   float4 *ycur;                   // transformed targets, current level order
   float4 *yorig;                  // transformed targets, original order
   int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s] (original target index)
-  int2 *ovf;                      // kept pairs beyond cap, row-major [s * ov + t] = {j, bits of a}
-  int ov;                         // overflow entries per row
+  int2 *ovf;                      // row lists: kept pair t of row s at [s * ov + t] = {j, bits of a}
+  int ov;                         // row-list entries per row
   const float *tf, *tl;           // target features / labels, original order (float4 chunks)
   const float2 *tg;               // target geometric types, original order
   int *nnz_row;                   // n
@@ -151,9 +151,9 @@ struct BatchDev {
   double *assoc_bytes;            // algorithmic bytes of the association passes
   int record_bytes;               // packed bytes of one target record
   // rows with more than `cap` kept pairs, {pair, row, kept count, 0}; reset by k_transform
-  int4 *sel_list;                 // cap < count <= cap + ov: select among ELL + overflow entries
+  int4 *sel_list;                 // cap < count <= ov: select from the row list
   int *sel_count;
-  int4 *scan_list;                // count > cap + ov: index-ordered rescan of the row
+  int4 *scan_list;                // count > ov: index-ordered rescan of the row
   int *scan_count;
 };
 

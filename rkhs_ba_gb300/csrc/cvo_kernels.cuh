@@ -168,10 +168,10 @@ __global__ void k_transform(BatchDev B) {
 // The reference keeps the first `cap` kept pairs of a row in ascending target
 // index (its scan stops at `cap`, src/cvo/CvoGPU.cu:994-996).  Here candidates
 // arrive in grid order, so k_assoc writes the first `cap` kept pairs of a row to
-// its ELL slots and the next `ov` to the row's overflow entries; a row that kept
-// more than `cap` is listed, and k_select (count <= cap + ov) or k_rescan
-// (count > cap + ov) rewrites its ELL row with the `cap` smallest kept indices,
-// i.e. the reference's set.
+// its ELL slots and the first `ov` to the row's list (row-major); a row that kept
+// more than `cap` is listed, and k_select (count <= ov) or k_rescan (count > ov)
+// rewrites its ELL row with the `cap` smallest kept indices, i.e. the
+// reference's set.
 struct EllRow {
   int *j;
   float *v;
@@ -307,11 +307,11 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
 }
 
 // Kept count of a finished row; a row with more than cap kept pairs is listed for
-// k_select (its overflow entries hold them all) or k_rescan.
+// k_select (its row list holds them all) or k_rescan.
 __device__ __forceinline__ void finish_row(const BatchDev &B, PairDev *P, int p, int s, int cnt, int cap, int ov) {
   P->nnz_row[s] = cnt < cap ? cnt : cap;
   if (cnt > cap && cap > 0) {
-    if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
+    if (cnt <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
     else B.scan_list[atomicAdd(B.scan_count, 1)] = make_int4(p, s, cnt, 0);
   }
 }
@@ -603,15 +603,14 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;   // source index of lane 0's row
   bool lost = false;
-  // kept pair number `slot` of row r enters its ELL slot (first cap) or overflow entry
+  // kept pair number `slot` of row r enters its ELL slot (first cap) and its row list
   auto put = [&](int r, int slot, int j, float a) {
     const size_t sidx = (size_t)(tile0 + r);
     if (slot < cap) {
       P->A_j[(size_t)slot * n + sidx] = j;
       P->A_v[(size_t)slot * n + sidx] = a;
-    } else if (slot - cap < ov) {
-      P->ovf[sidx * ov + (slot - cap)] = make_int2(j, __float_as_int(a));
     }
+    if (slot < ov) P->ovf[sidx * ov + slot] = make_int2(j, __float_as_int(a));
   };
   for (int pass = 0; pass < npass && !lost; pass++) {
     int x0, y0, z0, nx, ny, nz;
@@ -747,7 +746,7 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
 }
 
 // ------------------------------------------------------------ selection
-constexpr int kSelMax = 4096;      // ELL + overflow entries one row can hold (cap + ov)
+constexpr int kSelMax = 4096;      // kept pairs one row list can hold
 constexpr int kSelStage = 2048;    // rows up to this many entries are selected from shared memory
 constexpr int kSelThreads = 128;
 
@@ -778,12 +777,13 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
   write_row_sums(P->row_sums + (size_t)s * 8, P->mode, K, w0, w1, w2, v0, v1, v2, as);
 }
 
-// One warp per listed row with cap < count <= cap + ov: the row's cap ELL entries
-// and its overflow entries hold every kept pair.  A three-digit radix select
-// (8 + 8 + 6 bits of the 22-bit target index, warp-private histograms in shared
-// memory) finds the cap-th smallest index r; the entries with index <= r (exactly
-// cap, indices are distinct) are compacted into the ELL slots in entry order.
-// Indices are staged in shared memory when the row fits (kSelStage entries).
+// One warp per listed row with cap < count <= ov: the row list (row-major, kept
+// pairs in the order they were kept) holds every kept pair of the row.  A radix
+// select over the bits of the target index (8-bit digits from the highest bit
+// the pair's target count needs, warp-private histograms in shared memory) finds
+// the cap-th smallest index r; the entries with index <= r (exactly cap, indices
+// are distinct) are written to the ELL slots in list order.  Indices are staged
+// in shared memory when the row fits (kSelStage entries).
 __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
   __shared__ int hist_all[kSelThreads / 32][256];
@@ -796,22 +796,18 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     const int4 it = B.sel_list[e];
     const PairDev *P = &B.pairs[it.x];
     const int s = it.y, n = P->n, cap = P->cap, ov = P->ov;
-    const int E = cap + min(it.z - cap, ov);
-    const int2 *ovf = P->ovf + (size_t)s * ov;
+    const int E = it.z;
+    const int2 *lst = P->ovf + (size_t)s * ov;
     const bool staged = E <= kSelStage;
-    auto entry = [&](int t) -> int {
-      if (staged) return jb[t];
-      return t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
-    };
     if (staged) {
-      for (int t = lane; t < E; t += 32) jb[t] = t < cap ? P->A_j[(size_t)t * n + s] : ovf[t - cap].x;
+      for (int t = lane; t < E; t += 32) jb[t] = lst[t].x;
     }
     __syncwarp();
+    auto entry = [&](int t) -> int { return staged ? jb[t] : lst[t].x; };
+    const int bits = P->m > 1 ? 32 - __clz(P->m - 1) : 1;
     int prefix = 0, target = cap;
-    const int shifts[3] = {14, 6, 0}, widths[3] = {8, 8, 6};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const int sh = shifts[d], wd = widths[d], hs = sh + wd;
+    for (int hs = bits; hs > 0; hs -= 8) {
+      const int sh = max(hs - 8, 0), wd = hs - sh;
       for (int b = lane; b < 256; b += 32) hist[b] = 0;
       __syncwarp();
       for (int t = lane; t < E; t += 32) {
@@ -845,19 +841,17 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     int base = 0;
     for (int t0 = 0; t0 < E; t0 += 32) {
       const int t = t0 + lane;
-      int j = 0;
-      float a = 0.f;
+      int2 v = make_int2(0, 0);
       bool k = false;
       if (t < E) {
-        j = entry(t);
-        k = j <= r;
-        a = t < cap ? P->A_v[(size_t)t * n + s] : __int_as_float(ovf[t - cap].y);
+        v = lst[t];
+        k = v.x <= r;
       }
       const unsigned bal = __ballot_sync(FULLMASK, k);
       if (k) {
         const int c = base + __popc(bal & ((1u << lane) - 1u));
-        P->A_j[(size_t)c * n + s] = j;
-        P->A_v[(size_t)c * n + s] = a;
+        P->A_j[(size_t)c * n + s] = v.x;
+        P->A_v[(size_t)c * n + s] = __int_as_float(v.y);
       }
       base += __popc(bal);
     }
@@ -865,7 +859,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   }
 }
 
-// One warp per listed row with count > cap + ov: the reference's own order, i.e. a
+// One warp per listed row with count > ov: the reference's own order, i.e. a
 // scan of the targets by ascending original index (32 per step, one per lane) that
 // stops once cap pairs are kept.  Same per-pair arithmetic as k_assoc.
 template <int FCH, int LCH, bool GT>
