@@ -71,15 +71,13 @@ __device__ __forceinline__ int block_excl_scan(int v, int &excl, int (*scratch)[
   return total;
 }
 
+// One work item: the four tiles gw0 .. gw0 + 3 (one pair).
 template <int FCH, int LCH, bool GT>
-__global__ void __launch_bounds__(kCtaRows) k_assoc_cta(BatchDev B, KParams K) {
-  extern __shared__ __align__(128) unsigned char cta_smem[];
+__device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K, int gw0, unsigned char *cta_smem) {
   using D = CtaDense<FCH, LCH, GT>;
   constexpr int FP = D::FP, LP = D::LP;
   D &sm = *reinterpret_cast<D *>(cta_smem);
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-  const int gw0 = blockIdx.x * kCtaWarps;
-  if (gw0 >= B.total_warps) return;                 // the block's four tiles belong to one pair
   const int gw = gw0 + wib;
   const int p = find_segment(B.tile_off, B.npairs, gw0);
   PairDev *P = &B.pairs[p];
@@ -294,6 +292,23 @@ __global__ void __launch_bounds__(kCtaRows) k_assoc_cta(BatchDev B, KParams K) {
     if (ci0 >= ucells) break;
   }
   if (valid) finish_row(B, P, p, s, cnt, cap, P->ov);
+}
+
+// Persistent blocks take work items (four tiles each) from a counter, so blocks
+// that finish early pick up the remaining tiles.
+template <int FCH, int LCH, bool GT>
+__global__ void __launch_bounds__(kCtaRows) k_assoc_cta(BatchDev B, KParams K) {
+  extern __shared__ __align__(128) unsigned char cta_smem[];
+  __shared__ int item;
+  const int items = B.total_warps / kCtaWarps;
+  while (true) {
+    __syncthreads();   // every thread has read the previous item; shared memory is free
+    if (threadIdx.x == 0) item = atomicAdd(B.assoc_next, 1);
+    __syncthreads();
+    const int it = item;
+    if (it >= items) break;
+    assoc_block<FCH, LCH, GT>(B, K, it * kCtaWarps, cta_smem);
+  }
 }
 
 }  // namespace cvo_gb

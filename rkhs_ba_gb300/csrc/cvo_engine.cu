@@ -306,7 +306,7 @@ using AssocFn = void (*)(BatchDev, KParams);
 // chunks (C <= 20 or C <= 36, padded at upload), so the chunk counts below are
 // the storage strides of the clouds.
 template <int FC, int LC, bool G>
-static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem) {
+static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem, int &per_sm) {
   a = k_assoc_cta<FC, LC, G>;
   rs = k_rescan<FC, LC, G>;
   smem = CtaSmem<FC, LC, G>::kBytes;
@@ -322,17 +322,27 @@ static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem) {
     }
     set_mask |= bit;
   }
+  static int occ[64] = {0};
+  if (occ[dev & 63] == 0) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, a, kCtaRows, smem) != cudaSuccess || nb < 1) {
+      cudaGetLastError();
+      nb = 1;
+    }
+    occ[dev & 63] = nb;
+  }
+  per_sm = occ[dev & 63];
   return 0;
 }
 
-int select_kernels(const KParams &K, int F, int C, AssocFn &a, AssocFn &rs, size_t &smem) {
+int select_kernels(const KParams &K, int F, int C, AssocFn &a, AssocFn &rs, size_t &smem, int &per_sm) {
   int fch = K.use_int ? (F + 3) / 4 : 0;
   int lch = K.use_sem ? label_chunks(C) : 0;
   bool gt = K.use_gtype != 0;
   if (fch > 2 || lch > 9) return CVO_ERR_UNSUPPORTED;
 #define CVO_PICK(FC, LC)                                       \
   if (fch == FC && lch == LC) {                                \
-    return gt ? pick_assoc<FC, LC, true>(a, rs, smem) : pick_assoc<FC, LC, false>(a, rs, smem); \
+    return gt ? pick_assoc<FC, LC, true>(a, rs, smem, per_sm) : pick_assoc<FC, LC, false>(a, rs, smem, per_sm); \
   }
   CVO_PICK(0, 0) CVO_PICK(1, 0) CVO_PICK(2, 0)
   CVO_PICK(0, 5) CVO_PICK(1, 5) CVO_PICK(2, 5)
@@ -461,6 +471,7 @@ struct BatchHost {
   size_t assoc_smem = 0;
   int sel_blocks = 0;
   int ov = 0;
+  int assoc_per_sm = 1;
   int assoc_blocks = 0, xform_blocks = 0;
 };
 
@@ -474,7 +485,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     if (srcs[p]->F != F || tgts[p]->F != F || srcs[p]->C != C || tgts[p]->C != C) return CVO_ERR_INVALID_ARG;
     if (K.use_gtype && (!srcs[p]->has_geo || !tgts[p]->has_geo)) return CVO_ERR_INVALID_ARG;
   }
-  int rc = select_kernels(K, F, C, bh->assoc, bh->rescan, bh->assoc_smem);
+  int rc = select_kernels(K, F, C, bh->assoc, bh->rescan, bh->assoc_smem, bh->assoc_per_sm);
   if (rc) return rc;
   // grid levels per pair
   std::vector<std::vector<GridDesc>> lv(np);
@@ -540,7 +551,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   const int total_rows = bh->row_off[np];
   add(sizeof(PairDev) * np);
   add(sizeof(int) * (np + 1) * 5);
-  add(sizeof(int) * 6);
+  add(sizeof(int) * 7);
   add(sizeof(float) * np);
   add(sizeof(int4) * (size_t)total_rows);                        // selection list
   add(sizeof(int4) * (size_t)total_rows);                        // rescan list
@@ -600,7 +611,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   }
   PairDev *pairs_d = ar.take<PairDev>(np);
   int *offs_d = ar.take<int>((size_t)(np + 1) * 5);
-  int *ctr_d = ar.take<int>(6);
+  int *ctr_d = ar.take<int>(7);
   double *bytes_d = ar.take<double>(1);
   bh->src_max_norm = ar.take<float>(np);
   int4 *sel_list_d = ar.take<int4>(total_rows);
@@ -616,7 +627,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   int active = 0;
   for (int p = 0; p < np; p++) { mn[p] = srcs[p]->max_norm; if (!bh->pairs[p].done) active++; }
   CVO_CUDA_TRY(h, cudaMemcpyAsync(bh->src_max_norm, mn.data(), sizeof(float) * np, cudaMemcpyHostToDevice, h->stream));
-  int ctr_h[6] = {0, 0, active, 0, 0, 0};
+  int ctr_h[7] = {0, 0, active, 0, 0, 0, 0};
   CVO_CUDA_TRY(h, cudaMemcpyAsync(ctr_d, ctr_h, sizeof(ctr_h), cudaMemcpyHostToDevice, h->stream));
   CVO_CUDA_TRY(h, cudaMemsetAsync(bytes_d, 0, sizeof(double), h->stream));
   CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -642,11 +653,14 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   B.scan_list = scan_list_d;
   B.sel_count = ctr_d + 4;
   B.scan_count = ctr_d + 5;
+  B.assoc_next = ctr_d + 6;
   {
     int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
     B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
   }
-  bh->assoc_blocks = (B.total_warps * 32 + kAssocThreads - 1) / kAssocThreads;
+  // persistent association blocks: one wave of resident blocks (work items are taken from a counter)
+  bh->assoc_blocks = std::max(1, std::min(B.total_warps / kCtaWarps,
+                                          bh->assoc_per_sm * (h->num_sms > 0 ? h->num_sms : 152)));
   bh->xform_blocks = (B.total_targets + 255) / 256;
   bh->sel_blocks = std::max(1, std::min(h->num_sms > 0 ? 4 * h->num_sms : 608, (total_rows + 3) / 4));
   return 0;

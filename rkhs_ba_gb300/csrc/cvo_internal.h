@@ -155,6 +155,7 @@ struct BatchDev {
   int *sel_count;
   int4 *scan_list;                // count > ov: index-ordered rescan of the row
   int *scan_count;
+  int *assoc_next;                // next association work item (persistent blocks); reset by k_transform
 };
 
 // ------------------------------------------------------------- host side

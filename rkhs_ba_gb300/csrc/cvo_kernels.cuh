@@ -148,6 +148,7 @@ __global__ void k_transform(BatchDev B) {
     if (*B.active > 0) *B.active_iters += 1;
     *B.sel_count = 0;
     *B.scan_count = 0;
+    *B.assoc_next = 0;
   }
   if (gt >= B.total_targets) return;
   int p = find_segment(B.tgt_off, B.npairs, gt);
