@@ -35,6 +35,18 @@ METRIC = "registrations/s @50k pts: batched+learned vs plain grid, equal accurac
 UNIT = "registrations/s"
 
 
+def _profile_value(name, key):
+    """A `key: value` line of a committed profile summary (profiles/<name>), or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith(key + ":"):
+                return float(line.split(":", 1)[1])
+    return None
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -220,14 +232,17 @@ def run_ours(args):
         per_launch_bytes = prof["assoc_bytes"] / prof["assoc_launches"]
         avg_s = prof["assoc_ms"] / prof["assoc_launches"] / 1000.0
         achieved = per_launch_bytes / avg_s / 1e9
+        # DRAM bytes of one association launch: the ncu capture's bytes per pair
+        # (profiles/k_assoc_cta_global50k.md) times the mean number of pairs a launch
+        # of this run served (pair iterations / launches)
         traffic = None
-        tp = os.path.join(ROOT, "profiles", "assoc_traffic.json")
-        if os.path.exists(tp):
-            with open(tp) as fh:
-                traffic = json.load(fh).get("dram_bytes_per_launch")
+        pair_passes = sum(int(i) for _, its in results for i in its)
+        per_pair = _profile_value("k_assoc_cta_global50k.md", "dram_bytes_per_pair_launch")
+        if per_pair is not None and pair_passes > 0:
+            traffic = round(per_pair * pair_passes / prof["assoc_launches"])
         roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "k_assoc", "launches": prof["assoc_launches"],
+                "kernel": "k_assoc_cta + k_select + k_rescan + k_rowsum", "launches": prof["assoc_launches"],
                 "avg_launch_us": round(avg_s * 1e6, 3), "algorithmic_bytes_per_launch": round(per_launch_bytes),
                 "iteration_kernel_ms": {k: round(v, 3) for k, v in prof["kernel_ms"].items()}}
 

@@ -20,7 +20,6 @@ namespace cvo_gb {
 
 constexpr int kWarp = 32;
 constexpr int kMaxIndicatorWindow = 128;
-constexpr int kHist1Bits = 11;              // overflow radix-select, first digit
 constexpr int kMaxTargetBits = 22;          // targets per cloud <= 4M
 constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
 

@@ -1,11 +1,14 @@
 // cvo_kernels.cuh -- per-iteration kernels of the batched CVO engine.
 //
-// One iteration of the reference's align loop (src/cvo/CvoGPU.cu:1303-1433) is
-// four launches over every active pair of a batch:
+// One iteration of the reference's align loop (src/cvo/CvoGPU.cu:1303-1433) is a
+// fixed sequence of launches over every active pair of a batch:
 //   k_transform  target transform y' = R^T (y - T)            (CvoGPU_impl.cu:32-83)
-//   k_assoc      fused association: grid candidates -> kernel value -> threshold
-//                -> first-`cap`-by-index selection -> ELL row -> gradient partials
-//                                                               (CvoGPU.cu:951-1099, 2001-2062)
+//   k_assoc_cta  association: grid candidates -> tensor-core prefilter -> exact kernel
+//                value -> threshold -> ELL row (first cap) + row list
+//                (cvo_assoc_cta.cuh; per-warp path assoc_warp below)
+//                                                               (CvoGPU.cu:951-1099)
+//   k_select / k_rescan  rows with more than cap kept pairs: their cap smallest indices
+//   k_rowsum     per-row gradient partials from the final ELL    (CvoGPU.cu:2001-2062)
 //   k_reduce     per-pair FP64 sums of the row partials; gradient normalisation
 //                                                               (CvoGPU.cu:2065-2120)
 //   k_step       Taylor step-size terms over the ELL rows; the last block of each pair
