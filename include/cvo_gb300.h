@@ -227,6 +227,15 @@ int cvo_inner_product_noalloc(const cvo_params *p, const cvo_cloud *src_dev, con
 /* CvoGPU::compute_association_gpu (src/cvo/CvoGPU.cu:1836-1871). */
 int cvo_compute_association(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
                             const float T[16], float ell, cvo_assoc *out);
+/* CvoGPU::compute_association_gpu with a non-isotropic kernel (src/cvo/CvoGPU.cu:1936-1950,
+ * inner_product_non_isotropic_impl :1873-1934, fill_in_A_mat_gpu_dense_mat_kernel :719-830):
+ * kernel = 3x3 geometric kernel, column-major (Eigen::Matrix3f); it is inverted, rotated
+ * per source point (rotate_kernel_and_inverse, :135-160) and used as a Mahalanobis
+ * distance; no distance threshold, geometric type off.  Target moved by T^-1. */
+int cvo_compute_association_aniso(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                                  const float T[16], const float kernel[9], cvo_assoc *out);
+int cvo_compute_association_aniso_dev(cvo_handle *h, const cvo_gpu_cloud *src, const cvo_gpu_cloud *tgt,
+                                      const float T[16], const float kernel[9], cvo_assoc *out);
 int cvo_assoc_create(cvo_assoc **out);
 int cvo_assoc_destroy(cvo_assoc *a);
 /* Sizes of the stored association: rows (= source points), cols (= target points),

@@ -691,6 +691,127 @@ int orc_association(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *
   return r;
 }
 
+/* ============================================================ non-isotropic */
+/* compute_association_gpu with a 3x3 geometric kernel (src/cvo/CvoGPU.cu:1873-1950):
+ * the kernel is inverted once on the host (Eigen's 3x3 cofactor inverse: cofactors
+ * of column 0, det = their dot product with column 0, times 1/det), then for every
+ * source point a the inverse is rotated into a frame built from the point's
+ * direction (rotate_kernel_and_inverse, :135-160: z = a/|a|, x = (1, 1, -(z0+z1)/z2),
+ * y = z cross x, neither x nor y normalised, M = U K^-1 U^T with U = [x y z]) and
+ * d2 = (a-b)^T M (a-b) (mahananobis_distance, :165-183).  The pair value is
+ * sigma^2 exp(-d2/2) (no distance threshold, no range-scaled lengthscale) times the
+ * colour and semantic factors with their thresholds, geometric type off
+ * (fill_in_A_mat_gpu_dense_mat_kernel, :719-830); the first `cap` kept pairs of each
+ * row in ascending target index.  Arithmetic in float in the order written here. */
+void orc_kernel_inverse3(const float K[9], float Ki[9]) {
+  /* column-major in and out: K(r, c) = K[3 c + r] */
+#define KM(r, c) K[3 * (c) + (r)]
+  float cof[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+      float u = KM(i1, j1) * KM(i2, j2), v = KM(i1, j2) * KM(i2, j1);
+      cof[i][j] = u - v;
+    }
+  float d0 = cof[0][0] * KM(0, 0), d1 = cof[1][0] * KM(1, 0), d2 = cof[2][0] * KM(2, 0);
+  float det = (d0 + d1) + d2;
+  float invdet = 1.f / det;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) Ki[3 * j + i] = cof[j][i] * invdet;
+#undef KM
+}
+
+/* M (row-major) = U Ki U^T for source point x; Ki column-major. */
+void orc_aniso_row_matrix(const float Ki[9], const float x[3], float M[9]) {
+  float a = x[0] * x[0], b = x[1] * x[1], c = x[2] * x[2];
+  float nrm = sqrtf((a + b) + c);
+  float z[3] = {x[0] / nrm, x[1] / nrm, x[2] / nrm};
+  float t = -1.f / z[2];
+  float xv[3] = {1.f, 1.f, t * (z[0] + z[1])};
+  float yv[3];
+  yv[0] = z[1] * xv[2] - z[2] * xv[1];
+  yv[1] = z[2] * xv[0] - z[0] * xv[2];
+  yv[2] = z[0] * xv[1] - z[1] * xv[0];
+  float U[3][3];
+  for (int i = 0; i < 3; i++) { U[i][0] = xv[i]; U[i][1] = yv[i]; U[i][2] = z[i]; }
+  float P[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      float p0 = U[i][0] * Ki[3 * j + 0], p1 = U[i][1] * Ki[3 * j + 1], p2 = U[i][2] * Ki[3 * j + 2];
+      P[i][j] = (p0 + p1) + p2;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      float q0 = P[i][0] * U[j][0], q1 = P[i][1] * U[j][1], q2 = P[i][2] * U[j][2];
+      M[3 * i + j] = (q0 + q1) + q2;
+    }
+}
+
+static int pair_value_aniso(const kconst *k, const cvo_params *p, const float *x, const float *M, const float *fa,
+                            const float *la, const float *y, const float *fb, const float *lb, int F, int C,
+                            float *out) {
+  float kk = 1.f, ck = 1.f, sk = 1.f;
+  if (k->use_geo) {
+    float dl[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+    float v[3];
+    for (int j = 0; j < 3; j++) {
+      float v0 = dl[0] * M[3 * 0 + j], v1 = dl[1] * M[3 * 1 + j], v2 = dl[2] * M[3 * 2 + j];
+      v[j] = (v0 + v1) + v2;
+    }
+    float e0 = v[0] * dl[0], e1 = v[1] * dl[1], e2 = v[2] * dl[2];
+    float d2 = (e0 + e1) + e2;
+    kk = (float)((double)k->sigma2 * exp(-(double)d2 / 2.0));
+  }
+  if (k->use_int) {
+    float d2c = sqdist_n(fa, fb, F);
+    if (d2c < k->d2_c_thres) ck = (float)((double)k->c_sigma2 * exp(-(double)d2c / (2.0 * (double)k->c2)));
+    else return 0;
+  }
+  if (k->use_sem) {
+    float d2s = sqdist_n(la, lb, C);
+    if (d2s < k->d2_s_thres)
+      sk = (float)((double)(p->s_sigma * p->s_sigma) * exp(-(double)d2s / (2.0 * (double)k->s_ell * (double)k->s_ell)));
+    else return 0;
+  }
+  float ak = ck * kk * sk * 1.f;
+  if (ak > k->sp_thres) { *out = ak; return 1; }
+  return 0;
+}
+
+/* ELL (n x cap, row-major) of the non-isotropic kernel matrix at pose T (the target
+ * moved by T^-1, as the isotropic association). */
+int orc_association_aniso(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
+                          const float kernel[9], int cap, int *ind, float *val, int *nnz) {
+  int n = src->n, m = tgt->n, F = src->F, C = src->C;
+  kconst k = make_kconst(p);
+  float Ri[9], Ti[3], Ki[9];
+  orc_pose_to_rinv(T, Ri, Ti);
+  orc_kernel_inverse3(kernel, Ki);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)(m > 0 ? m : 1));
+  orc_transform(Ri, Ti, tgt, ytr);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i < n; i++) {
+    float x[3] = {cloud_x(src, i, 0), cloud_x(src, i, 1), cloud_x(src, i, 2)};
+    float M[9];
+    orc_aniso_row_matrix(Ki, x, M);
+    int cnt = 0;
+    for (int j = 0; j < m && cnt < cap; j++) {
+      float a;
+      if (pair_value_aniso(&k, p, x, M, F ? src->features + (size_t)i * F : NULL, C ? src->labels + (size_t)i * C : NULL,
+                           ytr + 3 * (size_t)j, F ? tgt->features + (size_t)j * F : NULL,
+                           C ? tgt->labels + (size_t)j * C : NULL, F, C, &a)) {
+        ind[(size_t)i * cap + cnt] = j;
+        val[(size_t)i * cap + cnt] = a;
+        cnt++;
+      }
+    }
+    for (int t = cnt; t < cap; t++) { ind[(size_t)i * cap + t] = -1; val[(size_t)i * cap + t] = 0.f; }
+    nnz[i] = cnt;
+  }
+  free(ytr);
+  return 0;
+}
+
 /* inner_product_cpu + se_kernel_init_ell_cpu (src/cvo/CvoGPU.cpp:113-231):
  * radius search with squared radius -2 l^2 ln(sp/sigma^2) (strict <, as
  * nanoflann's RadiusResultSet), no neighbour cap, no range ell, no colour or

@@ -57,6 +57,9 @@ def _lib():
             "orc_inner_product_cpu": (C.c_double, [vp, vp, vp, fp, C.c_float, C.POINTER(C.c_int64)]),
             "orc_function_angle": (C.c_double, [vp, vp, vp, fp, C.c_float, C.c_int, C.c_int]),
             "orc_association": (C.c_int, [vp, vp, vp, fp, C.c_float, C.c_int, ip, fp, ip]),
+            "orc_association_aniso": (C.c_int, [vp, vp, vp, fp, fp, C.c_int, ip, fp, ip]),
+            "orc_kernel_inverse3": (None, [fp, fp]),
+            "orc_aniso_row_matrix": (None, [fp, fp, fp]),
             "orc_nearest_init_pose": (C.c_int, [vp, vp, vp, C.c_float, fp, C.c_int, fp, fp]),
             "orc_num_threads": (C.c_int, []),
             "orc_set_num_threads": (None, [C.c_int]),
@@ -126,6 +129,40 @@ def association(params, src, tgt, T, ell, cap=None):
     _lib().orc_association(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), float(ell), int(cap),
                            ind.ctypes.data_as(C.POINTER(C.c_int)), val.ctypes.data_as(_fp),
                            nnz.ctypes.data_as(C.POINTER(C.c_int)))
+    return ind[:, :cap], val[:, :cap], nnz
+
+
+def kernel_inverse3(K):
+    """The oracle's float 3x3 inverse (cofactors of column 0, times 1/det); K, result (3, 3)."""
+    Kc = np.ascontiguousarray(np.asarray(K, np.float32).T.reshape(9))   # column-major
+    out = np.zeros(9, np.float32)
+    _lib().orc_kernel_inverse3(Kc.ctypes.data_as(_fp), out.ctypes.data_as(_fp))
+    return out.reshape(3, 3).T
+
+
+def aniso_row_matrix(Ki, x):
+    """M = U Ki U^T of rotate_kernel_and_inverse for source point x (row-major (3, 3))."""
+    Kc = np.ascontiguousarray(np.asarray(Ki, np.float32).T.reshape(9))
+    xv = np.ascontiguousarray(np.asarray(x, np.float32).reshape(3))
+    out = np.zeros(9, np.float32)
+    _lib().orc_aniso_row_matrix(Kc.ctypes.data_as(_fp), xv.ctypes.data_as(_fp), out.ctypes.data_as(_fp))
+    return out.reshape(3, 3)
+
+
+def association_aniso(params, src, tgt, T, kernel, cap=None):
+    """Non-isotropic kernel matrix (compute_association_gpu with a 3x3 kernel) as ELL:
+    (ind (n, cap), val (n, cap), nnz (n,)), the first cap kept pairs per row by index."""
+    cap = params.nearest_neighbors_max if cap is None else cap
+    n = src.num_points()
+    ind = np.zeros((n, max(cap, 1)), np.int32)
+    val = np.zeros((n, max(cap, 1)), np.float32)
+    nnz = np.zeros(n, np.int32)
+    s, t = src.c_struct(), tgt.c_struct()
+    Tm = _m16(T)
+    Kc = np.ascontiguousarray(np.asarray(kernel, np.float32).T.reshape(9))
+    _lib().orc_association_aniso(_pp(params), _pc(s), _pc(t), Tm.ctypes.data_as(_fp), Kc.ctypes.data_as(_fp),
+                                 int(cap), ind.ctypes.data_as(C.POINTER(C.c_int)), val.ctypes.data_as(_fp),
+                                 nnz.ctypes.data_as(C.POINTER(C.c_int)))
     return ind[:, :cap], val[:, :cap], nnz
 
 

@@ -86,6 +86,8 @@ SIGNATURES = {
     "cvo_function_angle": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _i, _i, _FP]),
     "cvo_inner_product_batch_dev": (_i, [_P, _P, _P, _i, _FP, _f, _FP]),
     "cvo_compute_association": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _P]),
+    "cvo_compute_association_aniso": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _FP, _P]),
+    "cvo_compute_association_aniso_dev": (_i, [_P, _P, _P, _FP, _FP, _P]),
     "cvo_assoc_create": (_i, [C.POINTER(_P)]),
     "cvo_assoc_destroy": (_i, [_P]),
     "cvo_assoc_info": (_i, [_P, _IP, _IP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

@@ -739,6 +739,34 @@ extern "C" int cvo_compute_association(cvo_handle *H, const cvo_cloud *src, cons
   return CVO_OK;
 }
 
+extern "C" int cvo_compute_association_aniso_dev(cvo_handle *H, const cvo_gpu_cloud *src, const cvo_gpu_cloud *tgt,
+                                                 const float T[16], const float kernel[9], cvo_assoc *out) {
+  if (!H || !src || !tgt || !T || !kernel || !out) return CVO_ERR_INVALID_ARG;
+  if (!H->h.stream) return CVO_ERR_CUDA;
+  std::vector<int> rowptr, col;
+  std::vector<float> val;
+  int rc = run_association_aniso(&H->h, src->d, tgt->d, T, kernel, H->h.params.nearest_neighbors_max, &rowptr, &col,
+                                 &val);
+  if (rc) return rc;
+  fill_assoc(out, src->d->n, tgt->d->n, rowptr, col, val);
+  return CVO_OK;
+}
+
+extern "C" int cvo_compute_association_aniso(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt,
+                                             const float T[16], const float kernel[9], cvo_assoc *out) {
+  if (!H || !src || !tgt || !T || !kernel || !out) return CVO_ERR_INVALID_ARG;
+  // compute_association_gpu returns without output for an empty cloud (CvoGPU.cu:1942-1943)
+  if (src->n == 0 || tgt->n == 0) { out->rows = src->n; out->cols = tgt->n; return CVO_OK; }
+  TmpClouds tc{H, {}};
+  cvo_gpu_cloud *s = nullptr, *t = nullptr;
+  int rc = cvo_cloud_upload(H, src, &s);
+  if (rc) return rc;
+  tc.v.push_back(s);
+  if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
+  tc.v.push_back(t);
+  return cvo_compute_association_aniso_dev(H, s, t, T, kernel, out);
+}
+
 // ------------------------------------------------------------ rotation grids
 namespace {
 

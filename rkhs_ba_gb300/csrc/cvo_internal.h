@@ -232,6 +232,12 @@ int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const 
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
                           const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out);
 
+// Non-isotropic association (cvo_aniso.cu): CSR of the kernel matrix with a 3x3
+// geometric kernel (column-major), first `cap` pairs per row in index order.
+void kernel_inverse3(const float K[9], float Ki[9]);
+int run_association_aniso(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], const float kernel[9],
+                          int cap, std::vector<int> *rowptr, std::vector<int> *col, std::vector<float> *val);
+
 // IRLS (cvo_irls.cu)
 int run_align_multi(Handle *h, int n_frames, DevCloud *const *clouds, double *poses, const uint8_t *hold_const,
                     int n_edges, const int *edges, double *secs, int *iters);

@@ -27,22 +27,9 @@ constexpr int kReduceRows = 1024;
 constexpr int kReduceThreads = 256;
 constexpr int kStepThreads = 256;
 constexpr int kPartStride = 12;
-constexpr float kBand = 2e-5f;      // relative band around sp_thres re-evaluated in double
 constexpr int kWaitLimit = 1 << 22; // mbarrier polls before a staged copy is declared lost
 
 // ------------------------------------------------------------ pair value
-// Exact kernel value as the reference computes it (double exp, float products);
-// used only for pairs whose fast FP32 value is within kBand of the threshold,
-// so it is kept out of line to keep the hot loop's register count low.
-__device__ __noinline__ float exact_value(const KParams &K, float l, float d2, float d2c, float d2s, float geo) {
-  float kk = 1.f, ck = 1.f, sk = 1.f;
-  if (K.use_geo) kk = __double2float_rn(dm((double)K.sigma2, exp(__ddiv_rn(-(double)d2, dm(dm(2.0, (double)l), (double)l)))));
-  if (K.use_int) ck = __double2float_rn(dm((double)K.c_sigma2, exp(__ddiv_rn(-(double)d2c, dm(2.0, (double)K.c2)))));
-  if (K.use_sem)
-    sk = __double2float_rn(dm((double)K.s_sigma_sq, exp(__ddiv_rn(-(double)d2s, dm(dm(2.0, (double)K.s_ell), (double)K.s_ell)))));
-  return fm(fm(fm(ck, kk), sk), geo);
-}
-
 // Kernel value of one (source, target) pair with the semantics of
 // fill_in_A_mat_gpu (src/cvo/CvoGPU.cu:996-1075).  `pre` is the lane's
 // participation; returns whether the pair is kept and its value in a.

@@ -302,12 +302,28 @@ class CvoGPU:
                 "cvo_function_angle", self._h)
         return out.value
 
-    def compute_association_gpu(self, source: CvoPointCloud, target: CvoPointCloud, T, ell: float) -> Association:
+    def compute_association_gpu(self, source, target, T, ell_or_kernel) -> Association:
+        """CvoGPU::compute_association_gpu, both overloads: a float lengthscale
+        (src/cvo/CvoGPU.cu:1836-1871) or a 3x3 non-isotropic geometric kernel
+        (:1936-1950, Eigen::Matrix3f; passed here as a (3, 3) array)."""
         ab = _AssocBuf()
-        s, t = source.c_struct(), target.c_struct()
         Ti = _m16(T)
-        L.check(L.lib().cvo_compute_association(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP), float(ell),
-                                                ab.h), "cvo_compute_association", self._h)
+        lib = L.lib()
+        K = np.asarray(ell_or_kernel, np.float32)
+        if K.ndim == 2:
+            Kc = np.ascontiguousarray(K.reshape(3, 3).T.reshape(9))   # column-major like Eigen
+            if isinstance(source, GpuCloud):
+                rc = lib.cvo_compute_association_aniso_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP),
+                                                           Kc.ctypes.data_as(_FP), ab.h)
+            else:
+                s, t = source.c_struct(), target.c_struct()
+                rc = lib.cvo_compute_association_aniso(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP),
+                                                       Kc.ctypes.data_as(_FP), ab.h)
+            L.check(rc, "cvo_compute_association_aniso", self._h)
+            return _read_assoc(ab.h)
+        s, t = source.c_struct(), target.c_struct()
+        L.check(lib.cvo_compute_association(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP),
+                                            float(ell_or_kernel), ab.h), "cvo_compute_association", self._h)
         return _read_assoc(ab.h)
 
     # -- global registration --------------------------------------------

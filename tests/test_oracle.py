@@ -132,6 +132,81 @@ def test_oracle_kernel_matrix_matches_numpy_restatement(cap):
         assert (nnz == 6).sum() > 10   # truncation exercised
 
 
+def _numpy_fill_A_aniso(p, src, ytr, cap, K):
+    """Independent numpy restatement of the non-isotropic kernel matrix
+    (fill_in_A_mat_gpu_dense_mat_kernel + rotate_kernel_and_inverse, src/cvo/CvoGPU.cu:
+    135-183, 719-830) on tiny inputs, float32 scalars in the canonical order, geometry only.
+    A source point with z = 0 makes -1/z2 infinite, so its row is NaN and keeps no pair,
+    as in the reference (the room's floor points exercise this)."""
+    f32 = np.float32
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        return _numpy_fill_A_aniso_rows(p, src, ytr, cap, K)
+
+
+def _numpy_fill_A_aniso_rows(p, src, ytr, cap, K):
+    f32 = np.float32
+    Ki = orc.kernel_inverse3(K)
+    sigma2 = f32(p.sigma) * f32(p.sigma)
+    out = []
+    for i in range(src.num_points()):
+        x = src.xyz[i].astype(f32)
+        nrm = np.sqrt((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2], dtype=f32)
+        z = [x[0] / nrm, x[1] / nrm, x[2] / nrm]
+        t = f32(-1.0) / z[2]
+        xv = [f32(1.0), f32(1.0), t * (z[0] + z[1])]
+        yv = [z[1] * xv[2] - z[2] * xv[1], z[2] * xv[0] - z[0] * xv[2], z[0] * xv[1] - z[1] * xv[0]]
+        U = [[xv[r], yv[r], z[r]] for r in range(3)]
+        P = [[(U[r][0] * Ki[0, c] + U[r][1] * Ki[1, c]) + U[r][2] * Ki[2, c] for c in range(3)] for r in range(3)]
+        M = [[(P[r][0] * U[c][0] + P[r][1] * U[c][1]) + P[r][2] * U[c][2] for c in range(3)] for r in range(3)]
+        row = []
+        for j in range(ytr.shape[0]):
+            if len(row) == cap:
+                break
+            y = ytr[j]
+            d = [x[0] - y[0], x[1] - y[1], x[2] - y[2]]
+            v = [(d[0] * M[0][c] + d[1] * M[1][c]) + d[2] * M[2][c] for c in range(3)]
+            d2 = (v[0] * d[0] + v[1] * d[1]) + v[2] * d[2]
+            k = f32(float(sigma2) * np.exp(-float(d2) / 2.0))
+            a = f32(f32(f32(1.0) * k) * f32(1.0)) * f32(1.0)
+            if a > f32(p.sp_thres):
+                row.append((j, a))
+        out.append(row)
+    return out
+
+
+@pytest.mark.parametrize("cap", [512, 4])
+def test_oracle_nonisotropic_matrix_matches_numpy_restatement(cap):
+    s0, t0, _ = scenes.room_pair(n=160, seed=6)
+    src, tgt = CvoPointCloud(s0.xyz * 0.1), CvoPointCloud(t0.xyz * 0.1)   # a 2 x 2 x 0.5 m room: dense rows
+    p = CvoParams(params_path("geometric"))
+    K = np.array([[0.5, 0.05, 0.0], [0.05, 0.4, 0.02], [0.0, 0.02, 0.6]], np.float32)
+    ytr = orc.transform_target(np.eye(4), tgt)
+    ind, val, nnz = orc.association_aniso(p, src, tgt, np.eye(4), K, cap=cap)
+    ref = _numpy_fill_A_aniso(p, src, ytr, cap, K)
+    total = 0
+    for i in range(src.num_points()):
+        assert nnz[i] == len(ref[i]), i
+        assert list(ind[i, :nnz[i]]) == [j for j, _ in ref[i]]
+        assert np.array_equal(val[i, :nnz[i]], np.array([a for _, a in ref[i]], np.float32))
+        total += nnz[i]
+    assert total > 0
+    if cap == 4:
+        assert (nnz == 4).sum() > 10   # index-ordered truncation exercised
+
+
+def test_oracle_kernel_inverse_and_rotated_kernel():
+    rng = np.random.default_rng(2)
+    A = rng.normal(size=(3, 3))
+    K = (A @ A.T + np.eye(3)).astype(np.float32)
+    assert np.allclose(orc.kernel_inverse3(K), np.linalg.inv(K.astype(np.float64)), rtol=1e-5, atol=1e-6)
+    x = np.array([0.7, -1.3, 2.1], np.float32)
+    z = x / np.linalg.norm(x)
+    xv = np.array([1.0, 1.0, -(z[0] + z[1]) / z[2]])
+    U = np.stack([xv, np.cross(z, xv), z], 1)          # x and y left unnormalised, as the reference
+    Ki = orc.kernel_inverse3(K)
+    assert np.allclose(orc.aniso_row_matrix(Ki, x), U @ Ki.astype(np.float64) @ U.T, rtol=1e-5, atol=1e-5)
+
+
 def test_gradient_is_derivative_of_inner_product():
     """d/ds <f(X), f(exp(-s xi) Y')> at s=0 equals sum_ij a_ij / l_i^2 (omega.(x x y) + v.(y - x))."""
     src, tgt, _ = scenes.room_pair(n=400, seed=2)
