@@ -157,6 +157,29 @@ int cvo_write_params(cvo_handle *h, const cvo_params *p);
 int cvo_cloud_upload(cvo_handle *h, const cvo_cloud *c, cvo_gpu_cloud **out);
 int cvo_cloud_free(cvo_handle *h, cvo_gpu_cloud *c);
 int cvo_cloud_size(const cvo_gpu_cloud *c);
+/* Feature and class counts of a device cloud and whether it has geometric types. */
+int cvo_cloud_dims(const cvo_gpu_cloud *c, int *F, int *C, int *has_geom_type);
+/* Copies a device cloud back in its original point order: xyz n x 3, features n x F,
+ * labels n x C, geom_type n x 2 (row-major floats); any pointer may be NULL.  The
+ * reference's counterpart is reading a CvoPointCloud's accessors (CvoPointCloud.hpp:32-221). */
+int cvo_cloud_download(cvo_handle *h, const cvo_gpu_cloud *c, float *xyz, float *features, float *labels,
+                       float *geom_type);
+/* CvoPointCloud(const ImageRGBD<float>&, const Calibration&, PointSelectionMethod)
+ * (src/utils/CvoPointCloud.cpp:458-560) with RawImage's intensity and gradient
+ * (src/utils/RawImage.cpp:9-45, 117-143), built on the device.  image: rows x cols x
+ * channels bytes (BGR for 3 channels, as cv::Mat); depth: rows x cols floats in raw
+ * units; intrinsic: fx, fy, cx, cy; scaling_factor: raw depth units per metre
+ * (Calibration::scaling_factor); uv: n_sel (u, v) selected pixels; geom_type: n_sel x 2
+ * or NULL (the selector's edge/surface weights); semantics: rows x cols x num_classes
+ * or NULL.  Features are B, G, R (or grey) / 255 and two gradient terms / 500 + 0.5;
+ * pixels without depth, non-finite points and points farther than 55 are dropped,
+ * the rest keep the selection order.  The image is used as given: the reference's
+ * default denoising (OpenCV fastNlMeans) and its pixel selectors (FAST, DSO, edges)
+ * are left to the caller.  *n_points receives the number of points kept. */
+int cvo_cloud_from_rgbd(cvo_handle *h, const uint8_t *image, int rows, int cols, int channels, const float *depth,
+                        const float intrinsic[4], float scaling_factor, const int *uv, int n_sel,
+                        const float *geom_type, int num_classes, const float *semantics, cvo_gpu_cloud **out,
+                        int *n_points);
 
 /* ------------------------------------------------------------- two-view */
 /* int CvoGPU::align(src, tgt, T_init, T_out&, Association*, double* secs, int* iters)

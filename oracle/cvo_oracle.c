@@ -691,6 +691,63 @@ int orc_association(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *
   return r;
 }
 
+/* ============================================================ RGB-D front-end */
+/* CvoPointCloud(const ImageRGBD<float>&, const Calibration&, ...) (src/utils/CvoPointCloud.cpp:458-560)
+ * with RawImage::compute_image_gradient (src/utils/RawImage.cpp:117-143).  Grey level of a
+ * BGR image: ITU-R BT.601 luma in 14-bit fixed point, (1868 B + 9617 G + 4899 R + 2^13) >> 14
+ * (OpenCV's 8-bit BGR2GRAY; OpenCV is a dependency absent here).  Features read the
+ * interleaved gradient array at the pixel index (the reference's indexing).  Returns the
+ * number of points kept; outputs sized for n_sel points. */
+int orc_cloud_from_rgbd(const unsigned char *img, int rows, int cols, int channels, const float *depth,
+                        const float intr[4], float scale, const int *uv, int n_sel, const float *geom, int C,
+                        const float *sem, float *oxyz, float *ofeat, float *olab, float *ogeo) {
+  size_t total = (size_t)rows * cols;
+  float *I = (float *)malloc(sizeof(float) * total);
+  float *grad = (float *)calloc(2 * total, sizeof(float));
+  for (size_t i = 0; i < total; i++) {
+    if (channels == 3) {
+      int b = img[3 * i], g = img[3 * i + 1], r = img[3 * i + 2];
+      I[i] = (float)((b * 1868 + g * 9617 + r * 4899 + (1 << 13)) >> 14);
+    } else {
+      I[i] = (float)img[i];
+    }
+  }
+  for (int idx = cols; idx < cols * (rows - 1); idx++) {
+    if (idx % cols == 0 || idx % cols == cols - 1) { grad[2 * idx] = 0.f; grad[2 * idx + 1] = 0.f; continue; }
+    float dx = 0.5f * (I[idx + 1] - I[idx - 1]);
+    float dy = 0.5f * (I[idx + cols] - I[idx - cols]);
+    if (!isfinite(dx)) dx = 0.f;
+    if (!isfinite(dy)) dy = 0.f;
+    grad[2 * idx] = dx;
+    grad[2 * idx + 1] = dy;
+  }
+  int F = channels + 2, nc = channels == 3 ? 3 : 1, k = 0;
+  for (int i = 0; i < n_sel; i++) {
+    int u = uv[2 * i], v = uv[2 * i + 1];
+    if (u < 0 || u >= cols || v < 0 || v >= rows) continue;
+    size_t pix = (size_t)v * cols + u;
+    float dep = depth[pix];
+    if (dep == 0.f || isnan(dep)) continue;
+    float z = dep / scale;
+    float x = ((float)u - intr[2]) * z / intr[0];
+    float y = ((float)v - intr[3]) * z / intr[1];
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) continue;
+    float a = x * x, b = y * y, c = z * z;
+    float nrm = sqrtf((a + b) + c);
+    if (nrm > 55.f) continue;
+    oxyz[3 * k] = x; oxyz[3 * k + 1] = y; oxyz[3 * k + 2] = z;
+    for (int t = 0; t < nc; t++) ofeat[(size_t)k * F + t] = (float)((double)img[pix * channels + t] / 255.0);
+    ofeat[(size_t)k * F + nc] = (float)((double)grad[pix] / 500.0 + 0.5);
+    ofeat[(size_t)k * F + nc + 1] = (float)((double)grad[pix + 1] / 500.0 + 0.5);
+    for (int t = 0; t < C; t++) olab[(size_t)k * C + t] = sem[pix * C + t];
+    if (geom) { ogeo[2 * k] = geom[2 * i]; ogeo[2 * k + 1] = geom[2 * i + 1]; }
+    k++;
+  }
+  free(I);
+  free(grad);
+  return k;
+}
+
 /* ============================================================ non-isotropic */
 /* compute_association_gpu with a 3x3 geometric kernel (src/cvo/CvoGPU.cu:1873-1950):
  * the kernel is inverted once on the host (Eigen's 3x3 cofactor inverse: cofactors

@@ -60,6 +60,8 @@ def _lib():
             "orc_association_aniso": (C.c_int, [vp, vp, vp, fp, fp, C.c_int, ip, fp, ip]),
             "orc_kernel_inverse3": (None, [fp, fp]),
             "orc_aniso_row_matrix": (None, [fp, fp, fp]),
+            "orc_cloud_from_rgbd": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, fp, fp, C.c_float, ip, C.c_int, vp,
+                                              C.c_int, vp, fp, fp, fp, fp]),
             "orc_nearest_init_pose": (C.c_int, [vp, vp, vp, C.c_float, fp, C.c_int, fp, fp]),
             "orc_num_threads": (C.c_int, []),
             "orc_set_num_threads": (None, [C.c_int]),
@@ -164,6 +166,31 @@ def association_aniso(params, src, tgt, T, kernel, cap=None):
                                  int(cap), ind.ctypes.data_as(C.POINTER(C.c_int)), val.ctypes.data_as(_fp),
                                  nnz.ctypes.data_as(C.POINTER(C.c_int)))
     return ind[:, :cap], val[:, :cap], nnz
+
+
+def cloud_from_rgbd(image, depth, intrinsic, scaling_factor, uv, geom_type=None, semantics=None):
+    """RGB-D frame + selected pixels -> (xyz (k, 3), features (k, F), labels (k, C), geom (k, 2) or None)."""
+    img = np.ascontiguousarray(image, np.uint8)
+    rows, cols = img.shape[:2]
+    ch = 1 if img.ndim == 2 else img.shape[2]
+    dep = np.ascontiguousarray(depth, np.float32)
+    intr = np.ascontiguousarray(intrinsic, np.float32)
+    uvc = np.ascontiguousarray(uv, np.int32).reshape(-1, 2)
+    n = uvc.shape[0]
+    Cn = 0 if semantics is None else semantics.shape[-1]
+    sem = None if semantics is None else np.ascontiguousarray(semantics, np.float32)
+    geo = None if geom_type is None else np.ascontiguousarray(geom_type, np.float32)
+    F = ch + 2
+    xyz = np.zeros((max(n, 1), 3), np.float32)
+    feat = np.zeros((max(n, 1), F), np.float32)
+    lab = np.zeros((max(n, 1), max(Cn, 1)), np.float32)
+    og = np.zeros((max(n, 1), 2), np.float32)
+    k = _lib().orc_cloud_from_rgbd(img.ctypes.data_as(C.c_void_p), rows, cols, ch, dep.ctypes.data_as(_fp),
+                                   intr.ctypes.data_as(_fp), float(scaling_factor), uvc.ctypes.data_as(C.POINTER(C.c_int)),
+                                   n, None if geo is None else geo.ctypes.data_as(C.c_void_p), Cn,
+                                   None if sem is None else sem.ctypes.data_as(C.c_void_p), xyz.ctypes.data_as(_fp),
+                                   feat.ctypes.data_as(_fp), lab.ctypes.data_as(_fp), og.ctypes.data_as(_fp))
+    return xyz[:k], feat[:k], lab[:k, :Cn], (og[:k] if geo is not None else None)
 
 
 def flow(params, src, ytr, ind, val, nnz):

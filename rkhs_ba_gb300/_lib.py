@@ -86,6 +86,10 @@ SIGNATURES = {
     "cvo_function_angle": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _i, _i, _FP]),
     "cvo_inner_product_batch_dev": (_i, [_P, _P, _P, _i, _FP, _f, _FP]),
     "cvo_compute_association": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _P]),
+    "cvo_cloud_dims": (_i, [_P, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    "cvo_cloud_download": (_i, [_P, _P, _FP, _FP, _FP, _FP]),
+    "cvo_cloud_from_rgbd": (_i, [_P, _P, _i, _i, _i, _FP, _FP, _f, C.POINTER(_i), _i, _FP, _i, _FP, C.POINTER(_P),
+                                 C.POINTER(_i)]),
     "cvo_compute_association_aniso": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _FP, _P]),
     "cvo_compute_association_aniso_dev": (_i, [_P, _P, _P, _FP, _FP, _P]),
     "cvo_assoc_create": (_i, [C.POINTER(_P)]),

@@ -358,6 +358,39 @@ extern "C" int cvo_cloud_free(cvo_handle *H, cvo_gpu_cloud *c) {
 
 extern "C" int cvo_cloud_size(const cvo_gpu_cloud *c) { return c && c->d ? c->d->n : 0; }
 
+extern "C" int cvo_cloud_dims(const cvo_gpu_cloud *c, int *F, int *C, int *has_geom_type) {
+  if (!c || !c->d) return CVO_ERR_INVALID_ARG;
+  if (F) *F = c->d->F;
+  if (C) *C = c->d->C;
+  if (has_geom_type) *has_geom_type = c->d->has_geo ? 1 : 0;
+  return CVO_OK;
+}
+
+extern "C" int cvo_cloud_download(cvo_handle *H, const cvo_gpu_cloud *c, float *xyz, float *features, float *labels,
+                                  float *geom_type) {
+  if (!H || !c || !c->d) return CVO_ERR_INVALID_ARG;
+  if (!H->h.stream) return CVO_ERR_CUDA;
+  return cloud_download(&H->h, c->d, xyz, features, labels, geom_type);
+}
+
+extern "C" int cvo_cloud_from_rgbd(cvo_handle *H, const uint8_t *image, int rows, int cols, int channels,
+                                   const float *depth, const float intrinsic[4], float scaling_factor, const int *uv,
+                                   int n_sel, const float *geom_type, int num_classes, const float *semantics,
+                                   cvo_gpu_cloud **out, int *n_points) {
+  if (!H || !out) return CVO_ERR_INVALID_ARG;
+  if (!H->h.stream) return CVO_ERR_CUDA;
+  DevCloud *d = nullptr;
+  int rc = cloud_from_rgbd(&H->h, image, rows, cols, channels, depth, intrinsic, scaling_factor, uv, n_sel, geom_type,
+                           num_classes, semantics, &d);
+  if (rc) {
+    if (d) cloud_free(d);
+    return rc;
+  }
+  *out = new cvo_gpu_cloud{d, H};
+  if (n_points) *n_points = d->n;
+  return CVO_OK;
+}
+
 namespace {
 
 struct TmpClouds {

@@ -142,43 +142,15 @@ int dalloc(Handle *h, T **p, size_t count) {
 
 }  // namespace
 
-int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
-  if (!c || !out) return CVO_ERR_INVALID_ARG;
-  if (c->n < 0 || c->F < 0 || c->C < 0) return CVO_ERR_INVALID_ARG;
-  if (c->n > 0 && (!c->xyz || (c->xyz_stride != 3 && c->xyz_stride != 4))) return CVO_ERR_INVALID_ARG;
-  if (c->F > 0 && c->n > 0 && !c->features) return CVO_ERR_INVALID_ARG;
-  if (c->C > 0 && c->n > 0 && !c->labels) return CVO_ERR_INVALID_ARG;
-  if (c->n > (1 << kMaxTargetBits)) return CVO_ERR_CAPACITY;
-  DevCloud *d = new DevCloud();
-  d->n = c->n; d->F = c->F; d->C = c->C;
-  d->FP = (c->F + 3) / 4 * 4;
-  d->CP = 4 * label_chunks(c->C);
-  d->has_geo = c->geom_type != nullptr;
-  int n = c->n;
+// Device part of a cloud's construction from staged device arrays (xyz with stride
+// 3 or 4, features n x F, labels n x C, geometric types n float2 or null) and its
+// bounding box: packed original-order records, Morton tile order, tile extents.
+static int cloud_build(Handle *h, DevCloud *d, const float *xyz_d, int stride, const float *feat_in,
+                       const float *lab_in, const float2 *geo_in, const float mn[3], const float mx[3]) {
+  const int n = d->n;
   int rc = 0;
-  // bounding box and largest range on the host (input is host memory)
-  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-  double maxn2 = 0;
-  for (int i = 0; i < n; i++) {
-    const float *p = c->xyz + (size_t)i * c->xyz_stride;
-    for (int k = 0; k < 3; k++) {
-      if (!std::isfinite(p[k])) { delete d; return CVO_ERR_INVALID_ARG; }
-      mn[k] = std::min(mn[k], p[k]);
-      mx[k] = std::max(mx[k], p[k]);
-    }
-    double n2 = (double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2];
-    maxn2 = std::max(maxn2, n2);
-  }
-  if (n == 0) { for (int k = 0; k < 3; k++) mn[k] = mx[k] = 0.f; }
-  for (int k = 0; k < 3; k++) { d->bbmin[k] = mn[k]; d->bbmax[k] = mx[k]; }
-  d->max_norm = (float)std::sqrt(maxn2) * (1.f + 1e-6f);
-  *out = d;
-  if (n == 0) return 0;
-
-  float *xyz_d = nullptr, *feat_in = nullptr, *lab_in = nullptr;
   int *perm_vals = nullptr, *perm_tmp = nullptr;
   unsigned int *keys = nullptr, *keys_tmp = nullptr;
-  size_t xyz_bytes = sizeof(float) * (size_t)n * c->xyz_stride;
   if ((rc = dalloc(h, &d->pos, n)) || (rc = dalloc(h, &d->feat, (size_t)n * d->FP)) ||
       (rc = dalloc(h, &d->lab, (size_t)n * d->CP)) || (rc = dalloc(h, &d->sperm, n)) ||
       (rc = dalloc(h, &d->spos, n)) || (rc = dalloc(h, &d->sfeat, (size_t)n * d->FP)) ||
@@ -187,28 +159,20 @@ int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
   if (d->has_geo) {
     if ((rc = dalloc(h, &d->geo, n)) || (rc = dalloc(h, &d->sgeo, n))) return rc;
   }
-  if ((rc = dalloc(h, &xyz_d, (size_t)n * c->xyz_stride))) return rc;
-  CVO_CUDA_TRY(h, cudaMemcpyAsync(xyz_d, c->xyz, xyz_bytes, cudaMemcpyHostToDevice, h->stream));
-  k_pack_positions<<<(n + 255) / 256, 256, 0, h->stream>>>(xyz_d, c->xyz_stride, n, d->pos);
+  k_pack_positions<<<(n + 255) / 256, 256, 0, h->stream>>>(xyz_d, stride, n, d->pos);
   h->launches++;
   if (d->FP > 0) {
-    if ((rc = dalloc(h, &feat_in, (size_t)n * c->F))) return rc;
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(feat_in, c->features, sizeof(float) * (size_t)n * c->F, cudaMemcpyHostToDevice,
-                                    h->stream));
     size_t tot = (size_t)n * d->FP;
-    k_pad_rows<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(feat_in, n, c->F, d->FP, d->feat);
+    k_pad_rows<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(feat_in, n, d->F, d->FP, d->feat);
     h->launches++;
   }
   if (d->CP > 0) {
-    if ((rc = dalloc(h, &lab_in, (size_t)n * c->C))) return rc;
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(lab_in, c->labels, sizeof(float) * (size_t)n * c->C, cudaMemcpyHostToDevice,
-                                    h->stream));
     size_t tot = (size_t)n * d->CP;
-    k_pad_rows<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(lab_in, n, c->C, d->CP, d->lab);
+    k_pad_rows<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(lab_in, n, d->C, d->CP, d->lab);
     h->launches++;
   }
   if (d->has_geo)
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(d->geo, c->geom_type, sizeof(float2) * n, cudaMemcpyHostToDevice, h->stream));
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(d->geo, geo_in, sizeof(float2) * n, cudaMemcpyDeviceToDevice, h->stream));
 
   // source tile order: Morton order of a 1024^3 lattice over the bounding box
   if ((rc = dalloc(h, &keys, n)) || (rc = dalloc(h, &keys_tmp, n)) || (rc = dalloc(h, &perm_vals, n)) ||
@@ -234,9 +198,129 @@ int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
   double es = 0.0;
   for (float e : ext_h) es += e;
   d->tile_ext = tiles > 0 ? (float)(es / tiles) : 0.f;
-  cudaFree(xyz_d); cudaFree(feat_in); cudaFree(lab_in);
   cudaFree(keys); cudaFree(keys_tmp); cudaFree(perm_vals); cudaFree(perm_tmp);
   return 0;
+}
+
+static DevCloud *new_cloud(int n, int F, int C, bool has_geo) {
+  DevCloud *d = new DevCloud();
+  d->n = n; d->F = F; d->C = C;
+  d->FP = (F + 3) / 4 * 4;
+  d->CP = 4 * label_chunks(C);
+  d->has_geo = has_geo;
+  return d;
+}
+
+static void set_extent(DevCloud *d, const float mn[3], const float mx[3], double maxn2) {
+  for (int k = 0; k < 3; k++) { d->bbmin[k] = mn[k]; d->bbmax[k] = mx[k]; }
+  d->max_norm = (float)std::sqrt(maxn2) * (1.f + 1e-6f);
+}
+
+int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
+  if (!c || !out) return CVO_ERR_INVALID_ARG;
+  if (c->n < 0 || c->F < 0 || c->C < 0) return CVO_ERR_INVALID_ARG;
+  if (c->n > 0 && (!c->xyz || (c->xyz_stride != 3 && c->xyz_stride != 4))) return CVO_ERR_INVALID_ARG;
+  if (c->F > 0 && c->n > 0 && !c->features) return CVO_ERR_INVALID_ARG;
+  if (c->C > 0 && c->n > 0 && !c->labels) return CVO_ERR_INVALID_ARG;
+  if (c->n > (1 << kMaxTargetBits)) return CVO_ERR_CAPACITY;
+  int n = c->n;
+  // bounding box and largest range on the host (input is host memory)
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  double maxn2 = 0;
+  for (int i = 0; i < n; i++) {
+    const float *p = c->xyz + (size_t)i * c->xyz_stride;
+    for (int k = 0; k < 3; k++) {
+      if (!std::isfinite(p[k])) return CVO_ERR_INVALID_ARG;
+      mn[k] = std::min(mn[k], p[k]);
+      mx[k] = std::max(mx[k], p[k]);
+    }
+    double n2 = (double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2];
+    maxn2 = std::max(maxn2, n2);
+  }
+  if (n == 0) { for (int k = 0; k < 3; k++) mn[k] = mx[k] = 0.f; }
+  DevCloud *d = new_cloud(n, c->F, c->C, c->geom_type != nullptr);
+  set_extent(d, mn, mx, maxn2);
+  *out = d;
+  if (n == 0) return 0;
+
+  float *xyz_d = nullptr, *feat_in = nullptr, *lab_in = nullptr;
+  float2 *geo_in = nullptr;
+  int rc = 0;
+  auto release = [&]() { cudaFree(xyz_d); cudaFree(feat_in); cudaFree(lab_in); cudaFree(geo_in); };
+  if ((rc = dalloc(h, &xyz_d, (size_t)n * c->xyz_stride))) { release(); return rc; }
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(xyz_d, c->xyz, sizeof(float) * (size_t)n * c->xyz_stride, cudaMemcpyHostToDevice,
+                                  h->stream));
+  if (d->FP > 0) {
+    if ((rc = dalloc(h, &feat_in, (size_t)n * c->F))) { release(); return rc; }
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(feat_in, c->features, sizeof(float) * (size_t)n * c->F, cudaMemcpyHostToDevice,
+                                    h->stream));
+  }
+  if (d->CP > 0) {
+    if ((rc = dalloc(h, &lab_in, (size_t)n * c->C))) { release(); return rc; }
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(lab_in, c->labels, sizeof(float) * (size_t)n * c->C, cudaMemcpyHostToDevice,
+                                    h->stream));
+  }
+  if (d->has_geo) {
+    if ((rc = dalloc(h, &geo_in, n))) { release(); return rc; }
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(geo_in, c->geom_type, sizeof(float2) * n, cudaMemcpyHostToDevice, h->stream));
+  }
+  rc = cloud_build(h, d, xyz_d, c->xyz_stride, feat_in, lab_in, geo_in, mn, mx);
+  release();
+  return rc;
+}
+
+// Bounding box (min, max per axis) and largest squared norm of n device points
+// (xyz stride 3), one block.
+__global__ void k_extent(const float *xyz, int n, float *box, double *maxn2) {
+  __shared__ float sl[3][256], sh[3][256];
+  __shared__ double sn[256];
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  double m2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float *p = xyz + 3 * (size_t)i;
+    for (int k = 0; k < 3; k++) { lo[k] = fminf(lo[k], p[k]); hi[k] = fmaxf(hi[k], p[k]); }
+    m2 = fmax(m2, (double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2]);
+  }
+  for (int k = 0; k < 3; k++) { sl[k][threadIdx.x] = lo[k]; sh[k][threadIdx.x] = hi[k]; }
+  sn[threadIdx.x] = m2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int t = 1; t < blockDim.x; t++) {
+      for (int k = 0; k < 3; k++) { lo[k] = fminf(lo[k], sl[k][t]); hi[k] = fmaxf(hi[k], sh[k][t]); }
+      m2 = fmax(m2, sn[t]);
+    }
+    for (int k = 0; k < 3; k++) { box[k] = lo[k]; box[3 + k] = hi[k]; }
+    *maxn2 = m2;
+  }
+}
+
+int cloud_from_device(Handle *h, int n, int F, int C, const float *xyz_d, const float *feat_d, const float *lab_d,
+                      const float2 *geo_d, DevCloud **out) {
+  if (n < 0 || F < 0 || C < 0 || !out) return CVO_ERR_INVALID_ARG;
+  if (n > (1 << kMaxTargetBits)) return CVO_ERR_CAPACITY;
+  float mn[3] = {0.f, 0.f, 0.f}, mx[3] = {0.f, 0.f, 0.f};
+  double maxn2 = 0.0;
+  if (n > 0) {
+    float *box = nullptr;
+    double *m2 = nullptr;
+    int rc = 0;
+    if ((rc = dalloc(h, &box, 6)) || (rc = dalloc(h, &m2, 1))) { cudaFree(box); return rc; }
+    k_extent<<<1, 256, 0, h->stream>>>(xyz_d, n, box, m2);
+    h->launches++;
+    float bh[6];
+    cudaError_t e = cudaMemcpyAsync(bh, box, sizeof(bh), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&maxn2, m2, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(box);
+    cudaFree(m2);
+    if (e != cudaSuccess) return set_cuda_error(h, e, "cloud extent");
+    for (int k = 0; k < 3; k++) { mn[k] = bh[k]; mx[k] = bh[3 + k]; }
+  }
+  DevCloud *d = new_cloud(n, F, C, geo_d != nullptr);
+  set_extent(d, mn, mx, maxn2);
+  *out = d;
+  if (n == 0) return 0;
+  return cloud_build(h, d, xyz_d, 3, feat_d, lab_d, geo_d, mn, mx);
 }
 
 void cloud_free(DevCloud *d) {

@@ -184,8 +184,18 @@ struct Handle {
 // Label rows are padded to 5 float4 chunks (C <= 20) or 9 chunks (C <= 36).
 inline int label_chunks(int C) { return C <= 0 ? 0 : (C <= 20 ? 5 : (C <= 36 ? 9 : (C + 3) / 4)); }
 
+// RGB-D frame -> device cloud, device cloud -> host arrays (cvo_frontend.cu)
+int cloud_from_rgbd(Handle *h, const uint8_t *image, int rows, int cols, int channels, const float *depth,
+                    const float intrinsic[4], float scaling_factor, const int *uv, int n_sel, const float *geom_type,
+                    int num_classes, const float *semantics, DevCloud **out);
+int cloud_download(Handle *h, const DevCloud *d, float *xyz, float *features, float *labels, float *geom_type);
+
 // grid / cloud management (cvo_grid.cu)
 int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out);
+// A cloud from device arrays (xyz n x 3, features n x F, labels n x C, geometric
+// types n float2 or null); the arrays stay owned by the caller.
+int cloud_from_device(Handle *h, int n, int F, int C, const float *xyz_d, const float *feat_d, const float *lab_d,
+                      const float2 *geo_d, DevCloud **out);
 void cloud_free(DevCloud *c);
 int cloud_level(Handle *h, DevCloud *c, int level_exp, GridDesc *host_desc);
 float level_cell_size(int level_exp);

@@ -103,12 +103,37 @@ class GpuCloud:
         cs = cloud.c_struct()
         L.check(L.lib().cvo_cloud_upload(cvo._h, C.byref(cs), C.byref(self._h)), "cvo_cloud_upload", cvo._h)
 
+    @classmethod
+    def _wrap(cls, cvo: "CvoGPU", handle: C.c_void_p) -> "GpuCloud":
+        g = cls.__new__(cls)
+        g._cvo = cvo
+        g.cloud = None
+        g._h = handle
+        return g
+
     @property
     def handle(self):
         return self._h
 
     def __len__(self):
         return L.lib().cvo_cloud_size(self._h)
+
+    def download(self) -> CvoPointCloud:
+        """The cloud's points, features, labels and geometric types copied back (original order)."""
+        F, Cn, hg = C.c_int(), C.c_int(), C.c_int()
+        lib = L.lib()
+        L.check(lib.cvo_cloud_dims(self._h, C.byref(F), C.byref(Cn), C.byref(hg)), "cvo_cloud_dims")
+        n = len(self)
+        xyz = np.zeros((n, 3), np.float32)
+        feat = np.zeros((n, F.value), np.float32)
+        lab = np.zeros((n, Cn.value), np.float32)
+        geo = np.zeros((n, 2), np.float32)
+        L.check(lib.cvo_cloud_download(self._cvo._h, self._h, xyz.ctypes.data_as(_FP),
+                                       feat.ctypes.data_as(_FP) if F.value else None,
+                                       lab.ctypes.data_as(_FP) if Cn.value else None,
+                                       geo.ctypes.data_as(_FP) if hg.value else None), "cvo_cloud_download",
+                self._cvo._h)
+        return CvoPointCloud(xyz, feat if F.value else None, lab if Cn.value else None, geo if hg.value else None)
 
     def free(self):
         if self._h:
@@ -206,6 +231,29 @@ class CvoGPU:
 
     def upload(self, cloud: CvoPointCloud) -> GpuCloud:
         return GpuCloud(self, cloud)
+
+    def cloud_from_rgbd(self, image, depth, intrinsic, scaling_factor, uv, geom_type=None, semantics=None) -> GpuCloud:
+        """CvoPointCloud(ImageRGBD, Calibration, ...) built on the device
+        (src/utils/CvoPointCloud.cpp:458-560): image (rows, cols[, 3]) uint8 BGR, depth
+        (rows, cols) raw units, intrinsic (fx, fy, cx, cy), uv (n, 2) selected pixels."""
+        img = np.ascontiguousarray(image, np.uint8)
+        rows, cols = img.shape[:2]
+        ch = 1 if img.ndim == 2 else img.shape[2]
+        dep = np.ascontiguousarray(depth, np.float32)
+        intr = np.ascontiguousarray(intrinsic, np.float32)
+        uvc = np.ascontiguousarray(uv, np.int32).reshape(-1, 2)
+        geo = None if geom_type is None else np.ascontiguousarray(geom_type, np.float32)
+        sem = None if semantics is None else np.ascontiguousarray(semantics, np.float32)
+        Cn = 0 if sem is None else sem.shape[-1]
+        out = C.c_void_p()
+        npts = C.c_int()
+        rc = L.lib().cvo_cloud_from_rgbd(self._h, img.ctypes.data_as(C.c_void_p), rows, cols, ch, dep.ctypes.data_as(_FP),
+                                         intr.ctypes.data_as(_FP), float(scaling_factor),
+                                         uvc.ctypes.data_as(C.POINTER(C.c_int)), uvc.shape[0],
+                                         None if geo is None else geo.ctypes.data_as(_FP), Cn,
+                                         None if sem is None else sem.ctypes.data_as(_FP), C.byref(out), C.byref(npts))
+        L.check(rc, "cvo_cloud_from_rgbd", self._h)
+        return GpuCloud._wrap(self, out)
 
     # -- two-view -------------------------------------------------------
     def align(self, source, target, T_init, want_association: bool = False):

@@ -207,6 +207,50 @@ def test_oracle_kernel_inverse_and_rotated_kernel():
     assert np.allclose(orc.aniso_row_matrix(Ki, x), U @ Ki.astype(np.float64) @ U.T, rtol=1e-5, atol=1e-5)
 
 
+def test_oracle_rgbd_front_end_matches_numpy_restatement():
+    """CvoPointCloud(ImageRGBD, Calibration) restated with numpy float32 scalars: BT.601
+    14-bit luma, central-difference gradient, back-projection, validity tests and the
+    reference's gradient-feature indexing (gradient[v w + u], gradient[v w + u + 1])."""
+    rng = np.random.default_rng(9)
+    rows, cols = 24, 31
+    img = rng.integers(0, 256, size=(rows, cols, 3), dtype=np.uint8)
+    depth = rng.uniform(500, 9000, size=(rows, cols)).astype(np.float32)
+    depth[3, 4] = 0.0
+    depth[5, 6] = np.nan
+    depth[7, 8] = 70000.0                     # 70 m: beyond the 55 m limit
+    uv = np.array([[u, v] for v in range(rows) for u in range(0, cols, 3)], np.int32)
+    uv = np.vstack([uv, [[4, 3], [6, 5], [8, 7]]]).astype(np.int32)
+    intr = np.array([300.0, 310.0, 15.2, 11.7], np.float32)
+    xyz, feat, lab, geo = orc.cloud_from_rgbd(img, depth, intr, 1000.0, uv)
+    f32 = np.float32
+    gray = ((img[..., 0].astype(np.int64) * 1868 + img[..., 1].astype(np.int64) * 9617 +
+             img[..., 2].astype(np.int64) * 4899 + 8192) >> 14).astype(np.float32).reshape(-1)
+    grad = np.zeros(2 * rows * cols, np.float32)
+    for idx in range(cols, cols * (rows - 1)):
+        if idx % cols in (0, cols - 1):
+            continue
+        grad[2 * idx] = f32(0.5) * (gray[idx + 1] - gray[idx - 1])
+        grad[2 * idx + 1] = f32(0.5) * (gray[idx + cols] - gray[idx - cols])
+    exp_xyz, exp_feat = [], []
+    for u, v in uv:
+        dep = depth[v, u]
+        if dep == 0 or np.isnan(dep):
+            continue
+        z = f32(dep) / f32(1000.0)
+        x = (f32(u) - intr[2]) * z / intr[0]
+        y = (f32(v) - intr[3]) * z / intr[1]
+        if np.sqrt((x * x + y * y) + z * z, dtype=np.float32) > f32(55.0):
+            continue
+        pix = v * cols + u
+        exp_xyz.append([x, y, z])
+        exp_feat.append([f32(img[v, u, 0] / 255.0), f32(img[v, u, 1] / 255.0), f32(img[v, u, 2] / 255.0),
+                         f32(float(grad[pix]) / 500.0 + 0.5), f32(float(grad[pix + 1]) / 500.0 + 0.5)])
+    assert xyz.shape[0] == len(exp_xyz)
+    assert len(exp_xyz) <= uv.shape[0] - 3      # the three invalid pixels are dropped
+    assert np.array_equal(xyz, np.array(exp_xyz, np.float32))
+    assert np.array_equal(feat, np.array(exp_feat, np.float32))
+
+
 def test_gradient_is_derivative_of_inner_product():
     """d/ds <f(X), f(exp(-s xi) Y')> at s=0 equals sum_ij a_ij / l_i^2 (omega.(x x y) + v.(y - x))."""
     src, tgt, _ = scenes.room_pair(n=400, seed=2)
