@@ -304,6 +304,112 @@ def cpu_baseline(args, pair, iters_per_reg, budget_s=None):
             "seconds_per_registration": round(per_reg, 3)}
 
 
+def run_component(args):
+    """Timing of one component beside the main workload (one JSON line): the multi-frame
+    window solve (8 frames of 20k-60k points, all 28 edges), the association with a
+    non-isotropic kernel (50k x 50k), or the RGB-D front-end (a 1226 x 370 frame, 50k
+    selected pixels).  Each call is timed end to end (host inputs, host outputs) after
+    warm-up; the CPU oracle is timed on a bounded sample of the same input."""
+    import torch
+    from oracle import oracle as orc
+    from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.mean(ts))
+
+    out = {"component": args.component, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "data": "synthetic (seeded scenes)", "dtype": "f32"}
+    if args.component == "irls":
+        clouds, gt = scenes.irls_window(n_frames=8, seed=0)
+        rng = np.random.default_rng(7)
+        P0 = []
+        for k in range(8):
+            T = gt[k].copy()
+            if k > 0:
+                T = T @ scenes.make_T(scenes.rot_axis_angle(rng.normal(size=3), np.radians(1.0)), rng.normal(size=3) * 0.03)
+            P0.append(T[:3, :].reshape(12))
+        P0 = np.stack(P0)
+        edges = [(a, b) for a in range(8) for b in range(a + 1, 8)]
+        hold = [1] + [0] * 7
+        p = CvoParams(params_path("irls"))
+        cvo = CvoGPU(params=p)
+        res = {}
+
+        def solve():
+            res["P"], res["s"], res["it"] = cvo.align_multi(clouds, P0, hold, edges)
+        sec = timed(solve)
+        q = p.copy()
+        q.multiframe_max_iters = 1
+        t0 = time.perf_counter()
+        orc.align_multi(q, clouds, P0, hold, edges)
+        t_outer = time.perf_counter() - t0
+        cpu_sec = t_outer * max(res["it"], 1)
+        out.update({"metric": "window solves/s (8 frames, 28 edges)", "unit": "solves/s", "value": round(1.0 / sec, 4),
+                    "ms_per_call": round(sec * 1000, 3),
+                    "config": {"frames": 8, "points_per_frame": [c.num_points() for c in clouds], "edges": 28,
+                               "params": "irls.yaml", "outer_iterations": int(res["it"])},
+                    "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "solves/s", "cores": cores, "kind": "port",
+                                     "sample": "one outer iteration of the oracle's window solve, scaled to the GPU "
+                                               "run's %d outer iterations" % res["it"]}})
+    elif args.component == "aniso":
+        src, tgt, _ = scenes.global_pair(n=args.points, seed=1000)
+        p = CvoParams(params_path("color"))
+        cvo = CvoGPU(params=p)
+        K = np.diag([0.5, 0.5, 0.6]).astype(np.float32)
+        T = np.eye(4, dtype=np.float32)
+        gs, gtc = cvo.upload(src), cvo.upload(tgt)
+        sec = timed(lambda: cvo.compute_association_gpu(gs, gtc, T, K))
+        nsub = min(2000, src.num_points())
+        from rkhs_ba_gb300 import CvoPointCloud
+        sub = CvoPointCloud(src.xyz[:nsub], src.features[:nsub])
+        t0 = time.perf_counter()
+        orc.association_aniso(p, sub, tgt, T, K)
+        cpu_sec = (time.perf_counter() - t0) * src.num_points() / nsub
+        out.update({"metric": "non-isotropic associations/s (50k x 50k)", "unit": "associations/s",
+                    "value": round(1.0 / sec, 4), "ms_per_call": round(sec * 1000, 3),
+                    "config": {"points": args.points, "kernel": "diag(0.5, 0.5, 0.6)", "params": "color.yaml",
+                               "device_clouds": True},
+                    "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "associations/s", "cores": cores,
+                                     "kind": "port", "sample": "%d source rows against all targets, scaled to %d rows"
+                                                               % (nsub, src.num_points())}})
+    elif args.component == "frontend":
+        rng = np.random.default_rng(3)
+        rows, cols = 370, 1226
+        yy, xx = np.mgrid[0:rows, 0:cols]
+        base = 127 + 80 * np.sin(xx / 9.0) * np.cos(yy / 7.0)
+        img = np.clip(base[..., None] + rng.normal(0, 25, size=(rows, cols, 3)), 0, 255).astype(np.uint8)
+        depth = np.exp(rng.uniform(np.log(2000.0), np.log(50000.0), size=(rows, cols))).astype(np.float32)
+        flat = rng.choice(rows * cols, size=50000, replace=False)
+        uv = np.stack([flat % cols, flat // cols], 1).astype(np.int32)
+        intr = np.array([718.0, 718.0, 613.0, 185.0], np.float32)
+        cvo = CvoGPU(params=CvoParams(params_path("color")))
+        sec = timed(lambda: cvo.cloud_from_rgbd(img, depth, intr, 1000.0, uv))
+        t0 = time.perf_counter()
+        orc.cloud_from_rgbd(img, depth, intr, 1000.0, uv)
+        cpu_sec = time.perf_counter() - t0
+        out.update({"metric": "RGB-D frames to clouds/s (1226 x 370, 50k points)", "unit": "frames/s",
+                    "value": round(1.0 / sec, 4), "ms_per_call": round(sec * 1000, 3),
+                    "config": {"rows": rows, "cols": cols, "selected": 50000, "host_inputs": True},
+                    "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "frames/s", "cores": 1, "kind": "port",
+                                     "sample": "the whole frame (the oracle is single-threaded here)"}})
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -346,10 +452,14 @@ def main():
     ap.add_argument("--ref-iters", type=float, default=251.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
+    ap.add_argument("--component", default="", choices=["", "irls", "aniso", "frontend"],
+                    help="time one component instead of the main workload")
     args = ap.parse_args()
     from rkhs_ba_gb300 import _build
     _build.build()
-    if args.impl == "reference":
+    if args.component:
+        run_component(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
