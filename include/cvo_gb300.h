@@ -296,6 +296,51 @@ int cvo_register_hypotheses_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud
                                 int n_hyp, const float *T_init, float judge_ell,
                                 float T_out[16], int *best, float *cos_out, double *secs);
 
+/* ---------------------------------------------------- learned proposal */
+/* A point-set network that proposes K = 8 poses per pair for global registration,
+ * standing in for the rotation grid of get_nearest_init_pose (src/cvo/CvoGPU.cpp:
+ * 367-398, grids :279-363), which stays the fallback.  No reference counterpart:
+ * the reference has no learned component.  Per-point MLP 8 -> 64 -> 128 (ReLU),
+ * max-pool over points_per_cloud sampled points, pair head 256 -> 256 -> K * 9
+ * (6D rotation + translation residual), BF16 tensor-core products with FP32
+ * accumulation; training (relaxed winner-takes-all loss, Adam) runs on the device.
+ * Poses are column-major 4x4 in cvo_align's T_init convention (target = R source + t). */
+typedef struct cvo_proposal cvo_proposal;
+int cvo_proposal_create(cvo_handle *h, int points_per_cloud, uint32_t seed, cvo_proposal **out);
+int cvo_proposal_destroy(cvo_proposal *p);
+/* parameter count, points per cloud and hypotheses per pair (p may be NULL) */
+int cvo_proposal_dims(const cvo_proposal *p, int *num_params, int *points_per_cloud, int *num_hyp);
+/* which: 0 weights, 1 gradients of the last training call, 2 / 3 Adam moments */
+int cvo_proposal_get(cvo_handle *h, cvo_proposal *p, int which, float *out);
+/* new weights (num_params floats); the Adam state restarts */
+int cvo_proposal_set(cvo_handle *h, cvo_proposal *p, const float *weights);
+/* One training step on n_pairs labelled pairs drawn from a device-resident pool:
+ * src_pts / tgt_pts are device arrays of n_scenes x n_pts x 8 floats (x, y, z and
+ * 5 features); pair b takes scene[b] and moves its target by T_label[b] (12 floats,
+ * row-major 3x4, target = R source + t), which is also its label.  Computes the
+ * loss (mean over pairs) and the gradients; with lr > 0 applies one Adam step. */
+int cvo_proposal_train_pool_dev(cvo_handle *h, cvo_proposal *p, int n_scenes, int n_pts, const float *src_pts,
+                                const float *tgt_pts, int n_pairs, const int *scene, const float *T_label,
+                                float lr, uint32_t seed, float *loss);
+/* Forward pass on pool pairs (T_tgt may be NULL = identity): raw_out n_pairs x 72
+ * network outputs, T_out n_pairs x 8 x 16 hypotheses (either may be NULL). */
+int cvo_proposal_forward_pool_dev(cvo_handle *h, cvo_proposal *p, int n_scenes, int n_pts, const float *src_pts,
+                                  const float *tgt_pts, int n_pairs, const int *scene, const float *T_tgt,
+                                  uint32_t seed, float *raw_out, float *T_out);
+/* Hypotheses for device clouds: T_out n_pairs x 8 x 16. */
+int cvo_proposal_hypotheses_dev(cvo_handle *h, cvo_proposal *p, int n_pairs, cvo_gpu_cloud *const *srcs,
+                                cvo_gpu_cloud *const *tgts, uint32_t seed, float *T_out);
+/* Learned global registration of n_pairs pairs: hypotheses ranked by the cos-angle
+ * at rank_ell, the best n_refine (1..8) of each pair refined by one batched align
+ * and judged by the final cos-angle at judge_ell; pairs judged below fallback_cos
+ * are registered again from the 24-rotation grid and keep the better result.
+ * T_out: n_pairs x 16 (cvo_align's T_out convention); cos_out, used_fallback and
+ * iters (align iterations summed over the pair's refinements) may be NULL. */
+int cvo_register_learned_batch_dev(cvo_handle *h, cvo_proposal *p, int n_pairs, cvo_gpu_cloud *const *srcs,
+                                   cvo_gpu_cloud *const *tgts, int n_refine, float rank_ell, float judge_ell,
+                                   float fallback_cos, uint32_t seed, float *T_out, float *cos_out,
+                                   int *used_fallback, int *iters, double *secs);
+
 /* ---------------------------------------------------------- multi-frame */
 /* CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670)
  * -> CvoBatchIRLS::solve (src/cvo/IRLS.cpp:148-367).  poses: n_frames*12 doubles

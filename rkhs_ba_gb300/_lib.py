@@ -100,6 +100,16 @@ SIGNATURES = {
     "cvo_get_nearest_init_pose_dev": (_i, [_P, _P, _P, _f, _i, _i, _FP, _DP]),
     "cvo_rotation_grid": (_i, [_i, _i, _FP, _i]),
     "cvo_register_hypotheses_dev": (_i, [_P, _P, _P, _i, _FP, _f, _FP, _IP, _FP, _DP]),
+    "cvo_proposal_create": (_i, [_P, _i, C.c_uint32, C.POINTER(_P)]),
+    "cvo_proposal_destroy": (_i, [_P]),
+    "cvo_proposal_dims": (_i, [_P, _IP, _IP, _IP]),
+    "cvo_proposal_get": (_i, [_P, _P, _i, _FP]),
+    "cvo_proposal_set": (_i, [_P, _P, _FP]),
+    "cvo_proposal_train_pool_dev": (_i, [_P, _P, _i, _i, _P, _P, _i, _IP, _FP, _f, C.c_uint32, _FP]),
+    "cvo_proposal_forward_pool_dev": (_i, [_P, _P, _i, _i, _P, _P, _i, _IP, _FP, C.c_uint32, _FP, _FP]),
+    "cvo_proposal_hypotheses_dev": (_i, [_P, _P, _i, C.POINTER(_P), C.POINTER(_P), C.c_uint32, _FP]),
+    "cvo_register_learned_batch_dev": (_i, [_P, _P, _i, C.POINTER(_P), C.POINTER(_P), _i, _f, _f, _f, C.c_uint32,
+                                            _FP, _FP, _IP, _IP, _DP]),
     "cvo_align_multi": (_i, [_P, _i, C.POINTER(CvoCloudC), _DP, C.POINTER(C.c_uint8), _i, _IP, _DP, _IP]),
     "cvo_align_multi_dev": (_i, [_P, _i, C.POINTER(_P), _DP, C.POINTER(C.c_uint8), _i, _IP, _DP, _IP]),
     "cvo_status_string": (C.c_char_p, [_i]),

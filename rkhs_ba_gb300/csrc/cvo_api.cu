@@ -996,6 +996,201 @@ extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
   return CVO_OK;
 }
 
+// ------------------------------------------------------ learned proposal
+struct cvo_proposal { NetDev *n; };
+
+extern "C" int cvo_proposal_create(cvo_handle *H, int points_per_cloud, uint32_t seed, cvo_proposal **out) {
+  if (!H || !out || points_per_cloud < 1 || points_per_cloud > 65536) return CVO_ERR_INVALID_ARG;
+  NetDev *n = nullptr;
+  int rc = net_create(&H->h, points_per_cloud, seed, &n);
+  if (rc) return rc;
+  *out = new cvo_proposal{n};
+  return CVO_OK;
+}
+
+extern "C" int cvo_proposal_destroy(cvo_proposal *p) {
+  if (!p) return CVO_OK;
+  net_destroy(p->n);
+  delete p;
+  return CVO_OK;
+}
+
+extern "C" int cvo_proposal_dims(const cvo_proposal *p, int *num_params, int *points_per_cloud, int *num_hyp) {
+  if (num_params) *num_params = (int)net_num_params();
+  if (points_per_cloud) *points_per_cloud = p ? net_points(p->n) : 0;
+  if (num_hyp) *num_hyp = 8;
+  return CVO_OK;
+}
+
+extern "C" int cvo_proposal_get(cvo_handle *H, cvo_proposal *p, int which, float *out) {
+  if (!H || !p || !out) return CVO_ERR_INVALID_ARG;
+  return net_get(&H->h, p->n, which, out);
+}
+
+extern "C" int cvo_proposal_set(cvo_handle *H, cvo_proposal *p, const float *weights) {
+  if (!H || !p || !weights) return CVO_ERR_INVALID_ARG;
+  return net_set(&H->h, p->n, weights);
+}
+
+extern "C" int cvo_proposal_train_pool_dev(cvo_handle *H, cvo_proposal *p, int n_scenes, int n_pts,
+                                           const float *src_pts, const float *tgt_pts, int n_pairs, const int *scene,
+                                           const float *T_label, float lr, uint32_t seed, float *loss) {
+  if (!H || !p) return CVO_ERR_INVALID_ARG;
+  return net_train_pool(&H->h, p->n, n_scenes, n_pts, src_pts, tgt_pts, n_pairs, scene, T_label, lr, seed, loss);
+}
+
+extern "C" int cvo_proposal_forward_pool_dev(cvo_handle *H, cvo_proposal *p, int n_scenes, int n_pts,
+                                             const float *src_pts, const float *tgt_pts, int n_pairs,
+                                             const int *scene, const float *T_tgt, uint32_t seed, float *raw_out,
+                                             float *T_out) {
+  if (!H || !p) return CVO_ERR_INVALID_ARG;
+  return net_forward_pool(&H->h, p->n, n_scenes, n_pts, src_pts, tgt_pts, n_pairs, scene, T_tgt, seed, raw_out,
+                          T_out);
+}
+
+static int collect_clouds(int n, cvo_gpu_cloud *const *a, std::vector<DevCloud *> *out) {
+  out->resize(n);
+  for (int i = 0; i < n; i++) {
+    if (!a[i]) return CVO_ERR_INVALID_ARG;
+    (*out)[i] = a[i]->d;
+  }
+  return 0;
+}
+
+extern "C" int cvo_proposal_hypotheses_dev(cvo_handle *H, cvo_proposal *p, int n_pairs, cvo_gpu_cloud *const *srcs,
+                                           cvo_gpu_cloud *const *tgts, uint32_t seed, float *T_out) {
+  if (!H || !p || n_pairs <= 0 || !srcs || !tgts || !T_out) return CVO_ERR_INVALID_ARG;
+  std::vector<DevCloud *> s, t;
+  int rc;
+  if ((rc = collect_clouds(n_pairs, srcs, &s)) || (rc = collect_clouds(n_pairs, tgts, &t))) return rc;
+  return net_hypotheses(&H->h, p->n, n_pairs, s.data(), t.data(), seed, T_out);
+}
+
+// Global registration of n_pairs pairs from the network's hypotheses: every pair's
+// K hypotheses are ranked by the approximate cos-angle at rank_ell (one batch for
+// all pairs), the best n_refine of each pair are refined by one batched align, and
+// the final cos-angle at judge_ell picks each pair's result.  A pair whose best
+// judged cos-angle stays below fallback_cos is registered again from the 24-rotation
+// grid (nearest grid rotation + align, judged the same way) and keeps the better of
+// the two.
+extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, int n_pairs,
+                                              cvo_gpu_cloud *const *srcs, cvo_gpu_cloud *const *tgts, int n_refine,
+                                              float rank_ell, float judge_ell, float fallback_cos, uint32_t seed,
+                                              float *T_out, float *cos_out, int *used_fallback, int *iters,
+                                              double *secs) {
+  constexpr int kHyp = 8;
+  if (!H || !p || n_pairs <= 0 || !srcs || !tgts || !T_out || n_refine < 1 || n_refine > kHyp)
+    return CVO_ERR_INVALID_ARG;
+  auto t0 = std::chrono::steady_clock::now();
+  Handle *h = &H->h;
+  std::vector<DevCloud *> s, t;
+  int rc;
+  if ((rc = collect_clouds(n_pairs, srcs, &s)) || (rc = collect_clouds(n_pairs, tgts, &t))) return rc;
+  for (int b = 0; b < n_pairs; b++)
+    if (s[b]->n == 0 || t[b]->n == 0) return CVO_ERR_EMPTY_CLOUD;
+  std::vector<float> hyp(16 * (size_t)n_pairs * kHyp);
+  if ((rc = net_hypotheses(h, p->n, n_pairs, s.data(), t.data(), seed, hyp.data()))) return rc;
+  const int cap = h->params.nearest_neighbors_max;
+  // rank the hypotheses of every pair (internal poses: the target moved by the inverse)
+  std::vector<int> pick;   // n_pairs * n_refine hypothesis indices
+  if (n_refine < kHyp) {
+    std::vector<DevCloud *> rs, rt;
+    for (int b = 0; b < n_pairs; b++)
+      for (int k = 0; k < kHyp; k++) {
+        rs.push_back(s[b]);
+        rt.push_back(t[b]);
+      }
+    std::vector<double> asum;
+    if ((rc = run_inner_product_pairs(h, rs, rt, hyp, rank_ell, cap, &asum))) return rc;
+    for (int b = 0; b < n_pairs; b++) {
+      std::vector<int> order(kHyp);
+      for (int k = 0; k < kHyp; k++) order[k] = k;
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int x, int y) { return asum[(size_t)b * kHyp + x] > asum[(size_t)b * kHyp + y]; });
+      for (int r = 0; r < n_refine; r++) pick.push_back(order[r]);
+    }
+  } else {
+    for (int b = 0; b < n_pairs; b++)
+      for (int k = 0; k < kHyp; k++) pick.push_back(k);
+  }
+  // refine the picked hypotheses in one batch, judge them in one batch
+  auto refine_and_judge = [&](const std::vector<int> &pairs_of, const std::vector<float> &inits,
+                              std::vector<float> *Tres, std::vector<float> *cosv, std::vector<int> *its) -> int {
+    std::vector<DevCloud *> as, at;
+    for (int b : pairs_of) {
+      as.push_back(s[b]);
+      at.push_back(t[b]);
+    }
+    BatchResult r;
+    int e = run_align_batch(h, as, at, inits, &r, nullptr, false, nullptr, nullptr, nullptr);
+    if (e) return e;
+    std::vector<float> Tj(inits.size());
+    for (size_t q = 0; q < pairs_of.size(); q++) rigid_inverse(&r.T_out[16 * q], &Tj[16 * q]);
+    std::vector<double> asum;
+    if ((e = run_inner_product_pairs(h, as, at, Tj, judge_ell, cap, &asum))) return e;
+    cosv->resize(pairs_of.size());
+    for (size_t q = 0; q < pairs_of.size(); q++) {
+      const int b = pairs_of[q];
+      (*cosv)[q] = (float)(asum[q] / (std::sqrt((double)s[b]->n) * std::sqrt((double)t[b]->n)));
+    }
+    *Tres = r.T_out;
+    *its = r.iters;
+    return 0;
+  };
+  std::vector<int> owner;
+  std::vector<float> inits;
+  for (int b = 0; b < n_pairs; b++)
+    for (int r = 0; r < n_refine; r++) {
+      owner.push_back(b);
+      const float *src = &hyp[16 * ((size_t)b * kHyp + pick[(size_t)b * n_refine + r])];
+      inits.insert(inits.end(), src, src + 16);
+    }
+  std::vector<float> Tr, cv;
+  std::vector<int> it;
+  if ((rc = refine_and_judge(owner, inits, &Tr, &cv, &it))) return rc;
+  std::vector<float> best_cos(n_pairs, -INFINITY);
+  std::vector<int> total_it(n_pairs, 0);
+  for (size_t q = 0; q < owner.size(); q++) {
+    const int b = owner[q];
+    total_it[b] += it[q];
+    if (cv[q] > best_cos[b]) {
+      best_cos[b] = cv[q];
+      copy16(&Tr[16 * q], T_out + 16 * (size_t)b);
+    }
+  }
+  // grid fallback for the pairs whose judged cos-angle stays low
+  std::vector<int> fb;
+  std::vector<float> fb_init;
+  for (int b = 0; b < n_pairs; b++) {
+    if (used_fallback) used_fallback[b] = 0;
+    if (!(best_cos[b] < fallback_cos)) continue;
+    float g[16], gi[16];
+    if ((rc = nearest_init_pose_impl(H, s[b], t[b], h->params.ell_init_first_frame, 0, 1, g, nullptr, nullptr)))
+      return rc;
+    rigid_inverse(g, gi);
+    fb.push_back(b);
+    fb_init.insert(fb_init.end(), gi, gi + 16);
+  }
+  if (!fb.empty()) {
+    if ((rc = refine_and_judge(fb, fb_init, &Tr, &cv, &it))) return rc;
+    for (size_t q = 0; q < fb.size(); q++) {
+      const int b = fb[q];
+      total_it[b] += it[q];
+      if (used_fallback) used_fallback[b] = 1;
+      if (cv[q] > best_cos[b]) {
+        best_cos[b] = cv[q];
+        copy16(&Tr[16 * q], T_out + 16 * (size_t)b);
+      }
+    }
+  }
+  for (int b = 0; b < n_pairs; b++) {
+    if (cos_out) cos_out[b] = best_cos[b];
+    if (iters) iters[b] = total_it[b];
+  }
+  if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return CVO_OK;
+}
+
 // ------------------------------------------------------------ multi-frame
 extern "C" int cvo_align_multi_dev(cvo_handle *H, int n_frames, cvo_gpu_cloud *const *clouds, double *poses,
                                    const uint8_t *hold_const, int n_edges, const int *edges, double *secs,

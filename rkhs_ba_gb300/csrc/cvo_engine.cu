@@ -875,6 +875,23 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
 
 // One association pass (no iteration) of one source/target pair under each of
 // the given poses (inner_product_impl, src/cvo/CvoGPU.cu:1673-1732).
+int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                            const std::vector<float> &T, float ell, int cap, std::vector<double> *asum) {
+  const int np = (int)srcs.size();
+  asum->assign(np, 0.0);
+  if (np == 0) return 0;
+  KParams K = make_kparams(h->params);
+  BatchHost bh;
+  std::vector<float> ell0(np, ell);
+  int rc = build_batch(h, K, srcs, tgts, T, MODE_IP, std::max(cap, 0), ell0, &bh);
+  if (rc) return rc;
+  launch_association(h, &bh, K);
+  if ((rc = check_err(h, &bh))) return rc;
+  if ((rc = read_pairs(h, &bh))) return rc;
+  for (int p = 0; p < np; p++) (*asum)[p] = bh.pairs[p].asum;
+  return 0;
+}
+
 int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::vector<float> &T, float ell, int cap,
                             std::vector<double> *asum, std::vector<long long> *nnz, bool export_assoc,
                             std::vector<int> *a_rowptr, std::vector<int> *a_cols, std::vector<float> *a_vals) {

@@ -224,6 +224,10 @@ int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::
                             bool export_assoc, std::vector<int> *a_rowptr_host, std::vector<int> *a_cols,
                             std::vector<float> *a_vals);
 
+// Inner products of independent (source, target, pose) triples in one batch.
+int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
+                            const std::vector<float> &T, float ell, int cap, std::vector<double> *asum);
+
 // One association pass per edge between world-frame clouds (multi-frame solver).
 // src_world: per edge, the source frame's points already in world coordinates in
 // tile order ({x, y, z, ||x||}); tgt_pose: per edge 12 floats, the target frame's
@@ -251,6 +255,21 @@ int run_association_aniso(Handle *h, DevCloud *src, DevCloud *tgt, const float T
 // IRLS (cvo_irls.cu)
 int run_align_multi(Handle *h, int n_frames, DevCloud *const *clouds, double *poses, const uint8_t *hold_const,
                     int n_edges, const int *edges, double *secs, int *iters);
+
+// Learned pose proposal (cvo_learn.cu)
+struct NetDev;
+size_t net_num_params();
+int net_create(Handle *h, int P, unsigned seed, NetDev **out);
+void net_destroy(NetDev *n);
+int net_points(const NetDev *n);
+int net_forward_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *src, const float *tgt, int Bn,
+                     const int *scene, const float *T_tgt, uint32_t seed, float *raw_out, float *T_out);
+int net_hypotheses(Handle *h, NetDev *n, int Bn, DevCloud *const *src, DevCloud *const *tgt, uint32_t seed,
+                   float *T_out);
+int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *src, const float *tgt, int Bn,
+                   const int *scene, const float *T_label, float lr, uint32_t seed, float *loss_out);
+int net_get(Handle *h, NetDev *n, int which, float *out);
+int net_set(Handle *h, NetDev *n, const float *in);
 
 // error helpers
 int set_cuda_error(Handle *h, cudaError_t e, const char *where);

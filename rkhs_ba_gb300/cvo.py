@@ -415,6 +415,32 @@ class CvoGPU:
                 "cvo_register_hypotheses_dev", self._h)
         return _from16(To), best.value, cos, secs.value
 
+    def register_learned_batch(self, net, sources, targets, n_refine: int = 2, rank_ell: float | None = None,
+                               judge_ell: float | None = None, fallback_cos: float = 0.0, seed: int = 0):
+        """Global registration of many pairs from the proposal network's hypotheses
+        (ranked, best n_refine refined in one batch, judged by the final cos-angle,
+        24-rotation grid fallback below fallback_cos).  Returns (T_out list of 4x4 in
+        align's output convention, cos (B,), used_fallback (B,), iters (B,), seconds)."""
+        p = self.get_params()
+        rank_ell = p.ell_init_first_frame if rank_ell is None else rank_ell
+        judge_ell = p.ell_init_first_frame if judge_ell is None else judge_ell
+        n = len(sources)
+        S = (C.c_void_p * n)(*[s.handle.value for s in sources])
+        Tg = (C.c_void_p * n)(*[t.handle.value for t in targets])
+        To = np.zeros(16 * n, np.float32)
+        cos = np.zeros(n, np.float32)
+        fb = np.zeros(n, np.int32)
+        its = np.zeros(n, np.int32)
+        secs = C.c_double(0)
+        L.check(L.lib().cvo_register_learned_batch_dev(self._h, net.handle, n, S, Tg, int(n_refine), float(rank_ell),
+                                                       float(judge_ell), float(fallback_cos),
+                                                       C.c_uint32(seed & 0xFFFFFFFF), To.ctypes.data_as(_FP),
+                                                       cos.ctypes.data_as(_FP),
+                                                       fb.ctypes.data_as(C.POINTER(C.c_int)),
+                                                       its.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs)),
+                "cvo_register_learned_batch_dev", self._h)
+        return [_from16(To[16 * i:16 * i + 16]) for i in range(n)], cos, fb, its, secs.value
+
     # -- multi-frame ----------------------------------------------------
     def align_multi(self, clouds, poses, hold_const, edges):
         """CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670).

@@ -225,9 +225,9 @@ def stereo_pair(n=50000, seed=0, max_yaw_deg=3.0, tz_range=(0.5, 1.5)):
     return CvoPointCloud(xs, fs), CvoPointCloud(xt, ft), inv_T(cam0) @ cam1
 
 
-def global_pair(n=50000, seed=0, max_trans=2.0):
-    """Config 5: stereo view resampled and moved by a uniformly random rotation and
-    a shift <= 2 m (target = G applied to an independent resample of the source view)."""
+def _global_views(n, seed):
+    """The two camera-frame views of a global pair (source, independent resample),
+    both centred on the source centroid, and the generator to draw the motion from."""
     rng = np.random.default_rng(seed)
     world = _TexturedWorld(rng)
     cam0 = np.eye(4)
@@ -235,8 +235,28 @@ def global_pair(n=50000, seed=0, max_trans=2.0):
     xr, fr = _stereo_view(world, cam0, np.random.default_rng(seed * 7919 + 2), n)
     # centre both clouds on the source centroid, as the reference's global benchmark centres its clouds
     c = xs.mean(0)
-    xs = xs - c
-    xr = xr - c
+    return xs - c, fs, xr - c, fr, rng
+
+
+def global_views(n=2048, seed=0):
+    """Unmoved view pair of a global scene as (n, 8) float32 arrays [xyz, 5 features]
+    for the proposal network's training pool; the motion is applied on the device."""
+    xs, fs, xr, fr, _ = _global_views(n, seed)
+    return (np.concatenate([xs, fs], 1).astype(np.float32), np.concatenate([xr, fr], 1).astype(np.float32))
+
+
+def random_motion(rng, max_trans=2.0):
+    """Row-major 3x4 [R | t] drawn like global_pair's motion (uniform rotation, shift <= max_trans)."""
+    R = random_rotation(rng)
+    d = rng.normal(size=3)
+    t = d / np.linalg.norm(d) * rng.uniform(0, max_trans)
+    return np.concatenate([R, t[:, None]], 1)
+
+
+def global_pair(n=50000, seed=0, max_trans=2.0):
+    """Config 5: stereo view resampled and moved by a uniformly random rotation and
+    a shift <= 2 m (target = G applied to an independent resample of the source view)."""
+    xs, fs, xr, fr, rng = _global_views(n, seed)
     R = random_rotation(rng)
     d = rng.normal(size=3)
     t = d / np.linalg.norm(d) * rng.uniform(0, max_trans)

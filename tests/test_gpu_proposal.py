@@ -1,0 +1,146 @@
+"""GPU checks of the learned pose proposal (rkhs_ba_gb300/csrc/cvo_learn.cu):
+
+* forward outputs and hypotheses against the oracle (oracle/proposal.py) with the
+  same bfloat16 operand rounding: max |diff| <= 1e-3 of the largest output;
+* loss and every gradient block of a training step against the oracle: loss within
+  1e-3 relative, gradient blocks within 1e-2 relative L2 (FP32 accumulation order
+  and the rare bfloat16 rounding it flips are the only differences);
+* the first Adam step against its closed form;
+* training on the device from a scene pool lowers the loss and the hypotheses'
+  rotation error on held-out scenes;
+* what the trained network gains: registration of held-out 50k-point-like pairs
+  (here 8k points) from its hypotheses against the plain 24-rotation grid, at equal
+  or better success with a fraction of the align work.
+"""
+import numpy as np
+import pytest
+
+from oracle import proposal as op
+from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
+from rkhs_ba_gb300.proposal import ProposalNet, ScenePool, evaluate, train
+
+pytestmark = pytest.mark.gpu
+
+P_SMALL = 96
+
+
+@pytest.fixture(scope="module")
+def cvo(cuda_device):
+    return CvoGPU(params=CvoParams(params_path("color")))
+
+
+@pytest.fixture(scope="module")
+def small_pool(cuda_device):
+    return ScenePool(*ScenePool.generate(4, 300, seed0=500, processes=1))
+
+
+def _batch(rng, n):
+    scene = rng.integers(0, 4, size=n)
+    T = np.stack([scenes.random_motion(rng) for _ in range(n)]).astype(np.float32)
+    return scene, T
+
+
+def test_forward_matches_oracle(cvo, small_pool):
+    net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=3)
+    rng = np.random.default_rng(2)
+    scene, T = _batch(rng, 5)
+    raw, hyp = net.forward_pool(small_pool, scene, T, seed=11)
+    X, cent = op.pool_batch(small_pool.host_src, small_pool.host_tgt, scene, T, 11, P_SMALL)
+    act = op.forward(net.weights(), X, len(scene), bf16_ops=True)
+    scale = float(np.abs(act["O"]).max())
+    assert np.abs(raw - act["O"]).max() <= 1e-3 * scale
+    H = op.hypotheses(raw, cent)
+    assert np.allclose(hyp[:, :, :3, :3], H[:, :, :3, :3], atol=1e-5)
+    assert np.allclose(hyp[:, :, :3, 3], H[:, :, :3, 3], atol=1e-4 * (1 + np.abs(H[:, :, :3, 3]).max()))
+
+
+def test_identity_motion_and_seed_change(cvo, small_pool):
+    net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=4)
+    a, _ = net.forward_pool(small_pool, [0, 1], None, seed=1)
+    b, _ = net.forward_pool(small_pool, [0, 1], np.tile(np.eye(4)[:3], (2, 1, 1)), seed=1)
+    c, _ = net.forward_pool(small_pool, [0, 1], None, seed=2)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+
+
+def test_gradients_match_oracle(cvo, small_pool):
+    net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=5)
+    rng = np.random.default_rng(3)
+    scene, T = _batch(rng, 6)
+    w = net.weights()
+    loss = net.train_step(small_pool, scene, T, lr=0.0, seed=7)
+    g = net.gradients()
+    assert np.array_equal(net.weights(), w)           # lr = 0: gradients only
+    loss_o, g_o, _, _ = op.train_step_grad(w, small_pool.host_src, small_pool.host_tgt, scene, T, 7, P_SMALL)
+    assert abs(loss - loss_o) <= 1e-3 * loss_o
+    gb, ob = op.unpack(g), op.unpack(g_o)
+    for name in gb:
+        err = np.linalg.norm(gb[name] - ob[name]) / max(np.linalg.norm(ob[name]), 1e-30)
+        assert err <= 1e-2, (name, err)
+    # the bfloat16 operands are the only approximation: the float64 gradients are close too
+    _, g64, _, _ = op.train_step_grad(w, small_pool.host_src, small_pool.host_tgt, scene, T, 7, P_SMALL,
+                                      bf16_ops=False)
+    assert np.linalg.norm(g - g64) / np.linalg.norm(g64) <= 5e-2
+
+
+def test_first_adam_step(cvo, small_pool):
+    net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=6)
+    rng = np.random.default_rng(4)
+    scene, T = _batch(rng, 4)
+    w0 = net.weights()
+    net.train_step(small_pool, scene, T, lr=0.0, seed=3)
+    g = net.gradients()
+    lr = 1e-3
+    net.train_step(small_pool, scene, T, lr=lr, seed=3)
+    w1 = net.weights()
+    # first step: m_hat = g, v_hat = g^2 -> w -= lr g / (|g| + 1e-8)
+    big = np.abs(g) > 1e-5 * np.abs(g).max()
+    expect = w0 - lr * g / (np.abs(g) + 1e-8)
+    assert np.allclose(w1[big], expect[big], atol=2e-6)
+    assert np.all(np.abs(w1 - w0) <= lr * 1.0001)
+
+
+@pytest.fixture(scope="module")
+def trained(cvo):
+    pool = ScenePool(*ScenePool.generate(300, 1024, seed0=2_000_000))
+    held = ScenePool(*ScenePool.generate(64, 1024, seed0=3_000_000))
+    net = ProposalNet(cvo, points_per_cloud=512, seed=0)
+    before, _ = evaluate(net, held, 64)
+    losses, secs = train(net, pool, steps=1500, batch=64, lr=1e-3, seed=0)
+    after, _ = evaluate(net, held, 64)
+    return net, losses, before, after, secs
+
+
+def test_training_on_the_device_learns_the_rotation(trained):
+    net, losses, before, after, secs = trained
+    assert np.all(np.isfinite(losses))
+    assert losses[-100:].mean() < 0.5 * losses[:100].mean()
+    assert np.median(after) < 20.0, np.median(after)
+    assert (after < 30.0).mean() >= 0.85
+    assert np.median(after) < 0.5 * np.median(before)
+
+
+def test_trained_network_gain_over_the_grid(cvo, trained):
+    """Held-out global pairs (uniform rotation, shift <= 2 m): the plain 24-rotation grid
+    (nearest grid rotation by cos-angle, then align) against the network's hypotheses
+    (best 2 of 8 by cos-angle refined in one batch, grid fallback)."""
+    net = trained[0]
+    pairs = [scenes.global_pair(n=8000, seed=4_000_000 + k) for k in range(8)]
+    gs = [cvo.upload(s) for s, _, _ in pairs]
+    gt = [cvo.upload(t) for _, t, _ in pairs]
+    p = cvo.get_params()
+    # plain grid
+    inits = []
+    for s, t in zip(gs, gt):
+        Tg, _ = cvo.get_nearest_init_pose(s, t, p.ell_init_first_frame, 0, 1)
+        inits.append(scenes.inv_T(Tg))
+    Tp, _, it_grid, _ = cvo.align_batch(gs, gt, inits)
+    ok_grid = [scenes.pose_error(Tp[k], pairs[k][2]) for k in range(len(pairs))]
+    # learned
+    Tl, cos, fb, it_learn, _ = cvo.register_learned_batch(net, gs, gt, n_refine=2)
+    ok_learn = [scenes.pose_error(Tl[k], pairs[k][2]) for k in range(len(pairs))]
+    succ = lambda errs: np.mean([r < 2.0 and t < 0.05 for r, t in errs])
+    assert succ(ok_learn) >= succ(ok_grid)
+    assert succ(ok_learn) >= 0.75
+    # the all-24 grid refines 24 hypotheses per pair; the network refines 2 (+ fallback)
+    assert fb.sum() <= 2
