@@ -1,16 +1,21 @@
 """Benchmark: global registration of 50k-point pairs on one GB300.
 
 Workload (one "step"): B seeded 50k-point pairs drawn like the colour/stereo
-configuration but with a uniformly random rotation and a shift <= 2 m; every pair
-is registered by the plain 24-rotation grid (cos-angle of each rotation at
-ell_init_first_frame, batched in one launch per pair), then all B pairs are refined
-together by the batched CVO align (one persistent batch, CUDA-graph chunks).
+configuration but with a uniformly random rotation and a shift <= 2 m.  Every pair
+is registered from the learned proposal: the network proposes 8 poses per pair, all
+pairs' hypotheses are ranked by the cos-angle in one batch, the best --refine of
+each pair are refined together by the batched CVO align (one persistent batch,
+CUDA-graph chunks) and judged by the final cos-angle, with the 24-rotation grid as
+the fallback below --fallback-cos.  The network is trained on the device before the
+timed region (or loaded with --proposal-weights).  The plain grid (nearest of the 24
+rotations by cos-angle, then the batched align) runs on the same pairs in the same
+process, and the grid with all 24 rotations refined runs on the first --all24-pairs.
 The metric is registrations/s; success = rotation error < 2 deg and translation
 error < 5 cm against the generated ground truth.
 
 value : device-resident clouds (inputs already in HBM), whole-job registrations/s
 e2e   : the same through the C ABI from host buffers (cloud upload inside the timed region)
-roofline : the fused association kernel (k_assoc), algorithmic bytes / event-timed duration
+roofline : the association phase of the CVO iteration, algorithmic bytes / event-timed duration
 cpu_baseline : the CPU oracle (a restatement of the reference's CPU inner product and
                align loop) on a bounded sample, scaled to registrations/s
 
@@ -117,6 +122,44 @@ def make_pairs(n_pairs, n_points, seed0=1000):
     return [scenes.global_pair(n=n_points, seed=seed0 + k) for k in range(n_pairs)]
 
 
+def _proposal(args, cvo):
+    """The learned proposal for the timed workload: weights from --proposal-weights when
+    given, else trained here on the device from a seeded scene pool (untimed setup)."""
+    from rkhs_ba_gb300.proposal import ProposalNet, ScenePool, evaluate, train
+    net = ProposalNet(cvo, points_per_cloud=512, seed=0)
+    info = {"points_per_cloud": 512, "hypotheses": net.num_hyp, "params": net.num_params}
+    if args.proposal_weights and os.path.exists(args.proposal_weights):
+        net.load(args.proposal_weights)
+        info["weights"] = os.path.basename(args.proposal_weights)
+        return net, info
+    t0 = time.perf_counter()
+    pool = ScenePool(*ScenePool.generate(args.train_scenes, 2048, seed0=1_000_000))
+    held = ScenePool(*ScenePool.generate(64, 2048, seed0=3_000_000))
+    info["pool_s"] = round(time.perf_counter() - t0, 2)
+    losses, secs = train(net, pool, steps=args.train_steps, batch=64, lr=1e-3, seed=0)
+    best, _ = evaluate(net, held, 64)
+    info.update({"train_scenes": args.train_scenes, "train_steps": args.train_steps, "batch": 64,
+                 "train_pairs": args.train_steps * 64, "train_s": round(secs, 2),
+                 "ms_per_train_step": round(1000.0 * secs / max(1, args.train_steps), 3),
+                 "loss_first_100": round(float(losses[:100].mean()), 4),
+                 "loss_last_100": round(float(losses[-100:].mean()), 4),
+                 "held_out_best_of_k_rot_err_deg_median": round(float(np.median(best)), 2),
+                 "held_out_best_of_k_within_30deg": round(float((best < 30).mean()), 3)})
+    if args.save_proposal:
+        net.save(args.save_proposal)
+    return net, info
+
+
+def _success(Ts, pairs):
+    errs = [scenes_pose_error(Ts[k], pairs[k][2]) for k in range(len(pairs))]
+    return [bool(r < 2.0 and t < 0.05) for r, t in errs]
+
+
+def scenes_pose_error(T, T_gt):
+    from rkhs_ba_gb300 import scenes
+    return scenes.pose_error(T, T_gt)
+
+
 def run_ours(args):
     import torch
     from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
@@ -137,28 +180,46 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     cvo.set_stream(stream.cuda_stream)
+    net, prop_info = _proposal(args, cvo)
     pairs = make_pairs(args.pairs, args.points, seed0=1000 + 100 * rank)
-    grid = CvoGPU.rotation_grid(1)  # 24-rotation grid
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
 
-    def register(gs, gt):
+    def register_learned(gs, gt):
+        Ts, cos, fb, its, _ = cvo.register_learned_batch(net, gs, gt, n_refine=args.refine,
+                                                         fallback_cos=args.fallback_cos)
+        return Ts, its, fb
+
+    def register_grid(gs, gt):
         inits = []
         for s, t in zip(gs, gt):
             T, _ = cvo.get_nearest_init_pose(s, t, p.ell_init_first_frame, 0, 1)
             inits.append(scenes.inv_T(T))        # CvoGPU::align(int overload) inverts the grid pose
         Ts, rets, its, _ = cvo.align_batch(gs, gt, inits)
-        return Ts, its
+        return Ts, its, np.zeros(len(gs), np.int32)
+
+    def timed(fn, gs, gt, steps):
+        ms, res = [], []
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res.append(fn(gs, gt))
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms, res
 
     gs = [cvo.upload(s) for s, _, _ in pairs]
     gt = [cvo.upload(t) for _, t, _ in pairs]
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
 
     for _ in range(args.warmup):
-        register(gs, gt)
+        register_learned(gs, gt)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
 
-    # ---- device-resident timed region
+    # ---- device-resident timed region: learned proposal + batched CVO
     cvo.profile(True)
     cvo.profile_reset()
     launches0 = cvo.kernel_launches
@@ -167,19 +228,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    step_ms = []
-    results = []
     t_wall0 = time.perf_counter()
-    for k in range(args.steps):
-        flush.fill_(float(k))
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        Ts, its = register(gs, gt)
-        e1.record(stream)
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-        results.append((Ts, its))
+    step_ms, results = timed(register_learned, gs, gt, args.steps)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -195,19 +245,52 @@ def run_ours(args):
         total_ms = float(t.item())
     n_reg = args.pairs * args.steps * world
     value = n_reg / (total_ms / 1000.0)
+    Ts, its, fb = results[-1]
+    succ = _success(Ts, pairs)
 
-    # accuracy of the last step
-    succ = []
-    iters = []
-    for (Ts, its) in results[-1:]:
-        for k, (_, _, T_gt) in enumerate(pairs):
-            r, tr = scenes.pose_error(Ts[k], T_gt)
-            succ.append(r < 2.0 and tr < 0.05)
-            iters.append(int(its[k]))
+    # ---- the plain 24-rotation grid (nearest grid rotation by cos-angle, then align) on the same pairs
+    register_grid(gs, gt)
+    grid_ms, grid_res = timed(register_grid, gs, gt, max(1, args.grid_steps))
+    grid_value = args.pairs * len(grid_ms) / (float(np.sum(grid_ms)) / 1000.0)
+    grid_succ = _success(grid_res[-1][0], pairs)
+    # ---- the plain grid with every one of its 24 rotations refined and judged (the
+    # grid's best accuracy), on the first --all24-pairs pairs
+    all24 = None
+    if args.all24_pairs > 0:
+        grid = CvoGPU.rotation_grid(1)
+        T24 = []
+        for R in grid:
+            T = np.eye(4)
+            T[:3, :3] = R.T                      # internal pose of grid rotation R
+            T24.append(T)
+        k24 = min(args.all24_pairs, args.pairs)
+        ms24, ok24, it24 = [], [], []
+        all24_err = None
+        for k in range(k24):
+            flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            try:
+                To, bi, cosv, _ = cvo.register_hypotheses(gs[k], gt[k], T24, p.ell_init_first_frame)
+            except RuntimeError as e:                 # reported in the line, not fatal to it
+                all24_err = str(e)
+                break
+            e1.record(stream)
+            e1.synchronize()
+            ms24.append(e0.elapsed_time(e1))
+            r, tr = scenes.pose_error(To, pairs[k][2])
+            ok24.append(bool(r < 2.0 and tr < 0.05))
+        if ms24:
+            all24 = {"value": round(len(ms24) / (float(np.sum(ms24)) / 1000.0), 4), "unit": UNIT,
+                     "pairs": len(ms24), "success_rate": float(np.mean(ok24)),
+                     "note": "24 aligns per pair in one batch, judged by the final cos-angle"}
+        if all24_err:
+            all24 = dict(all24 or {}, error=all24_err)
 
-    # ---- end-to-end through the C ABI from host buffers
+    # ---- end-to-end through the C ABI from host buffers (learned pipeline)
     h2d = sum(s.xyz.nbytes + s.features.nbytes + t.xyz.nbytes + t.features.nbytes for s, t, _ in pairs)
-    d2h = args.pairs * (16 * 4 + 24 * 4)
+    d2h = args.pairs * (16 * 4 + 4 + 4 + 4)
     torch.cuda.synchronize()
     e2e_ms = []
     for k in range(max(1, min(args.steps, 2))):
@@ -217,7 +300,7 @@ def run_ours(args):
         e0.record(stream)
         hs = [cvo.upload(s) for s, _, _ in pairs]
         ht = [cvo.upload(t) for _, t, _ in pairs]
-        register(hs, ht)
+        register_learned(hs, ht)
         e1.record(stream)
         e1.synchronize()
         e2e_ms.append(e0.elapsed_time(e1))
@@ -236,7 +319,7 @@ def run_ours(args):
         # (profiles/k_assoc_cta_global50k.md) times the mean number of pairs a launch
         # of this run served (pair iterations / launches)
         traffic = None
-        pair_passes = sum(int(i) for _, its in results for i in its)
+        pair_passes = sum(int(i) for r in results for i in r[1])
         per_pair = _profile_value("k_assoc_cta_global50k.md", "dram_bytes_per_pair_launch")
         if per_pair is not None and pair_passes > 0:
             traffic = round(per_pair * pair_passes / prof["assoc_launches"])
@@ -249,13 +332,20 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-        "config": {"workload": "global registration, plain 24-rotation grid + batched CVO refine",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16 operands, f32 accumulation)",
+        "data": "synthetic (seeded scenes)",
+        "config": {"workload": "global registration, learned proposal (8 hypotheses, best %d refined) + batched CVO, "
+                               "24-rotation grid fallback" % args.refine,
                    "points_per_cloud": args.points, "pairs_per_step": args.pairs, "params": "color.yaml",
-                   "rotation": "uniform SO(3)", "translation_max_m": 2.0,
+                   "rotation": "uniform SO(3)", "translation_max_m": 2.0, "fallback_cos": args.fallback_cos,
                    "l2": "256 MB buffer written between timed steps", "parallelism": "replicas"},
-        "accuracy": {"success_rate": float(np.mean(succ)) if succ else None, "criterion": "rot<2deg, trans<5cm",
-                     "mean_iters": float(np.mean(iters)) if iters else None},
+        "accuracy": {"success_rate": float(np.mean(succ)), "criterion": "rot<2deg, trans<5cm",
+                     "mean_iters": float(np.mean(its)), "fallbacks": int(np.sum(fb))},
+        "plain_grid": {"value": round(grid_value, 4), "unit": UNIT, "success_rate": float(np.mean(grid_succ)),
+                       "mean_iters": float(np.mean(grid_res[-1][1])), "steps": len(grid_ms),
+                       "note": "nearest of the 24 grid rotations by cos-angle, then one batched align"},
+        "plain_grid_all24": all24,
+        "proposal": prop_info,
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -264,7 +354,7 @@ def run_ours(args):
         "wall_s": round(wall, 3),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, pairs[0], float(np.mean(iters)) if iters else 100.0)
+        out["cpu_baseline"] = cpu_baseline(args, pairs[0], float(np.mean(grid_res[-1][1])))
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -451,6 +541,15 @@ def main():
     # same algorithm takes on this workload (251 on the 8 seeded pairs)
     ap.add_argument("--ref-iters", type=float, default=251.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--refine", type=int, default=1, help="hypotheses refined per pair (1..8)")
+    ap.add_argument("--fallback-cos", type=float, default=0.0,
+                    help="judged cos-angle below which a pair falls back to the grid")
+    ap.add_argument("--train-scenes", type=int, default=600)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--proposal-weights", default="", help="load the proposal network instead of training it")
+    ap.add_argument("--save-proposal", default="", help="save the trained proposal network (.npy)")
+    ap.add_argument("--grid-steps", type=int, default=1, help="timed steps of the plain grid")
+    ap.add_argument("--all24-pairs", type=int, default=2, help="pairs registered by the all-24 grid")
     ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
     ap.add_argument("--component", default="", choices=["", "irls", "aniso", "frontend"],
                     help="time one component instead of the main workload")

@@ -114,50 +114,9 @@ __device__ __forceinline__ int warp_maxi(int v) {
   return v;
 }
 
-// ---------------------------------------------------- bulk copies (TMA)
-// 1-D bulk copies global -> shared completed on an mbarrier (cp.async.bulk,
-// sm_90+).  Source, destination and size must be multiples of 16 bytes.
+// Shared-memory address of a generic pointer (for ldmatrix).
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
-}
-
-// Makes prior generic-proxy accesses of this thread to shared memory ordered
-// before later async-proxy (bulk copy) accesses, and mbarrier inits visible.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, uint32_t bytes, uint64_t *mbar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst_smem)),
-      "l"(src_gmem), "r"(bytes), "r"(smem_addr(mbar))
-      : "memory");
-}
-
-// Waits for the given phase parity of an mbarrier; gives up after `limit`
-// polls (each try_wait suspends for a hardware-defined time) and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int limit) {
-  uint32_t a = smem_addr(mbar);
-  for (int i = 0; i < limit; i++) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
 }
 
 constexpr float kBand = 2e-5f;      // relative band around sp_thres re-evaluated in double

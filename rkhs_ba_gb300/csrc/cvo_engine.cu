@@ -10,6 +10,7 @@
 #include <cstring>
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include "cvo_internal.h"
 #include "cvo_kernels.cuh"
 #include "cvo_assoc_cta.cuh"

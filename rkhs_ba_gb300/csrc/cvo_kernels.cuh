@@ -27,7 +27,6 @@ constexpr int kReduceRows = 1024;
 constexpr int kReduceThreads = 256;
 constexpr int kStepThreads = 256;
 constexpr int kPartStride = 12;
-constexpr int kWaitLimit = 1 << 22; // mbarrier polls before a staged copy is declared lost
 
 // ------------------------------------------------------------ pair value
 // Kernel value of one (source, target) pair with the semantics of
@@ -174,8 +173,7 @@ struct EllRow {
 // ------------------------------------------------------- candidate staging
 // A chunk of up to CH candidate targets in shared memory.  The grid stores the
 // members of one cell contiguously (positions, features, labels, geometric
-// types), so one chunk is 1-4 contiguous 16-byte-aligned ranges that a single
-// lane copies with bulk copies (the TMA unit) completed on an mbarrier.
+// types); the warp fills a chunk from consecutive cells with 16-byte loads.
 template <int FCH, int LCH, bool GT>
 struct __align__(16) StageBuf {
   static constexpr int CH = (LCH > 5) ? 16 : 32;
@@ -185,24 +183,28 @@ struct __align__(16) StageBuf {
   float4 geo[GT ? CH : 1];
 };
 
+// Copies the nk grid-order candidates t0 .. t0+nk-1 into slots at .. at+nk-1 of a
+// staging buffer; the warp copies each array (positions, features, labels,
+// geometric types) as one contiguous run of 16-byte vectors.
 template <int FCH, int LCH, bool GT>
-struct StageRec {
-  static constexpr uint32_t kBytes = 16u * (1 + FCH + LCH + (GT ? 1 : 0));   // staged bytes per candidate
-};
-
-// Copies `nk` grid-order candidates starting at t0 into slots [at, at + nk) of a
-// staging buffer (positions, features, labels, geometric types), completing on mbar.
-template <int FCH, int LCH, bool GT>
-__device__ __forceinline__ void stage_piece(StageBuf<FCH, LCH, GT> &buf, uint64_t *mbar, const float4 *ycur,
-                                            const GridDesc &G, int at, int t0, int nk) {
-  bulk_g2s(buf.pos + at, ycur + t0, 16u * nk, mbar);
-  if (FCH > 0)
-    bulk_g2s(buf.feat + (size_t)at * FCH, reinterpret_cast<const float4 *>(G.feat) + (size_t)t0 * FCH,
-             16u * FCH * nk, mbar);
-  if (LCH > 0)
-    bulk_g2s(buf.lab + (size_t)at * LCH, reinterpret_cast<const float4 *>(G.lab) + (size_t)t0 * LCH,
-             16u * LCH * nk, mbar);
-  if (GT) bulk_g2s(buf.geo + at, G.geo + t0, 16u * nk, mbar);
+__device__ __forceinline__ void stage_piece(StageBuf<FCH, LCH, GT> &buf, const float4 *ycur, const GridDesc &G,
+                                            int at, int t0, int nk, int lane) {
+#pragma unroll 1
+  for (int i = lane; i < nk; i += 32) buf.pos[at + i] = __ldg(ycur + t0 + i);
+  if (FCH > 0) {
+    const float4 *src = reinterpret_cast<const float4 *>(G.feat) + (size_t)t0 * FCH;
+#pragma unroll 1
+    for (int i = lane; i < nk * FCH; i += 32) buf.feat[at * FCH + i] = __ldg(src + i);
+  }
+  if (LCH > 0) {
+    const float4 *src = reinterpret_cast<const float4 *>(G.lab) + (size_t)t0 * LCH;
+#pragma unroll 1
+    for (int i = lane; i < nk * LCH; i += 32) buf.lab[at * LCH + i] = __ldg(src + i);
+  }
+  if (GT) {
+#pragma unroll 1
+    for (int i = lane; i < nk; i += 32) buf.geo[at + i] = __ldg(G.geo + t0 + i);
+  }
 }
 
 // ------------------------------------------------- tensor-core prefilter
@@ -308,7 +310,7 @@ __device__ __forceinline__ void finish_row(const BatchDev &B, PairDev *P, int p,
 }
 
 // Dynamic shared memory of one k_assoc block: per warp two staging buffers, the
-// prefilter tile, the grid descriptor and two mbarriers (16-byte aligned pieces).
+// prefilter tile and the grid descriptor (16-byte aligned pieces).
 template <int FCH, int LCH, bool GT>
 struct AssocSmem {
   static constexpr int kWarps = kAssocThreads / 32;
@@ -317,8 +319,7 @@ struct AssocSmem {
   static constexpr size_t kMma = align16(kStage + sizeof(StageBuf<FCH, LCH, GT>) * 2 * kWarps);
   static constexpr size_t kRows = align16(kMma + sizeof(MmaTile) * kWarps);
   static constexpr size_t kGrid = align16(kRows + sizeof(SrcRows<FCH, LCH>) * kWarps);
-  static constexpr size_t kMbar = align16(kGrid + sizeof(GridDesc) * kWarps);
-  static constexpr size_t kBytes = align16(kMbar + sizeof(uint64_t) * 2 * kWarps);
+  static constexpr size_t kBytes = align16(kGrid + sizeof(GridDesc) * kWarps);
 };
 
 // Plane p of a row/candidate block: entry i at base[p * stride + i] (16 B = 8 halves).
@@ -499,26 +500,18 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
   MmaTile *mma_all = reinterpret_cast<MmaTile *>(assoc_smem + L::kMma);
   SrcRows<FCH, LCH> *rows_all = reinterpret_cast<SrcRows<FCH, LCH> *>(assoc_smem + L::kRows);
   GridDesc *grid_all = reinterpret_cast<GridDesc *>(assoc_smem + L::kGrid);
-  uint64_t(*mbar_all)[2] = reinterpret_cast<uint64_t(*)[2]>(assoc_smem + L::kMbar);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   Buf *stage = stage_all[wib];
   MmaTile &mt = mma_all[wib];
   SrcRows<FCH, LCH> &sr = rows_all[wib];
-  uint64_t *mbar = mbar_all[wib];
   if (gw >= B.total_warps) return;
   const int p = find_segment(B.tile_off, B.npairs, gw);
   PairDev *P = &B.pairs[p];
   if (P->done) return;
-  if (lane == 0) {
-    grid_all[wib] = P->levels[P->level];
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    fence_proxy_async_smem();
-  }
+  if (lane == 0) grid_all[wib] = P->levels[P->level];
   __syncwarp();
   const GridDesc &G = grid_all[wib];
-  uint32_t parity[2] = {0u, 0u};
   const int n = P->n;
   const int s = (gw - B.tile_off[p]) * 32 + lane;
   const bool valid = s < n;
@@ -593,7 +586,6 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
   const float4 *__restrict__ ycur = P->ycur;
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;   // source index of lane 0's row
-  bool lost = false;
   // kept pair number `slot` of row r enters its ELL slot (first cap) and its row list
   auto put = [&](int r, int slot, int j, float a) {
     const size_t sidx = (size_t)(tile0 + r);
@@ -603,7 +595,7 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
     }
     if (slot < ov) P->ovf[sidx * ov + slot] = make_int2(j, __float_as_int(a));
   };
-  for (int pass = 0; pass < npass && !lost; pass++) {
+  for (int pass = 0; pass < npass; pass++) {
     int x0, y0, z0, nx, ny, nz;
     bool me = valid;
     if (per_lane) {
@@ -628,7 +620,7 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
     const float slack = 1e-3f * G.h;
     const float prune_r2 = (brq + slack) * (brq + slack);
     const int ncells = nx * ny * nz;
-    for (int cb = 0; cb < ncells && !lost; cb += 32) {
+    for (int cb = 0; cb < ncells; cb += 32) {
       int ci = cb + lane;
       int2 se = make_int2(0, 0);
       if (ci < ncells) {
@@ -647,59 +639,30 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
       unsigned mk = __ballot_sync(FULLMASK, se.y > 0);
       if (!mk) continue;
       // Chunks of up to CH candidates filled from consecutive non-empty cells of this
-      // batch; the warp walks a cursor (cell, offset) in lockstep and lane 0 issues
-      // one bulk copy set per piece.
+      // batch; the warp walks a cursor (cell, offset) in lockstep.
       int c_start = 0, c_cnt = 0, c_off = 0;
       auto fill = [&](int bi) -> int {
-        unsigned m2 = mk;
-        int n2 = c_cnt, o2 = c_off, filled = 0;
+        int filled = 0;
         while (filled < CH) {
-          if (o2 >= n2) {
-            if (!m2) break;
-            const int bb = __ffs(m2) - 1;
-            m2 &= m2 - 1;
-            n2 = __shfl_sync(FULLMASK, se.y, bb);
-            o2 = 0;
-          }
-          const int take = min(CH - filled, n2 - o2);
-          filled += take;
-          o2 += take;
-        }
-        if (filled == 0) return 0;
-        if (lane == 0) {
-          fence_proxy_async_smem();   // the lanes' reads of this buffer precede the copies into it
-          mbar_arrive_expect_tx(&mbar[bi], StageRec<FCH, LCH, GT>::kBytes * (uint32_t)filled);
-        }
-        int at = 0;
-        while (at < filled) {
           if (c_off >= c_cnt) {
+            if (!mk) break;
             const int bb = __ffs(mk) - 1;
             mk &= mk - 1;
             c_start = __shfl_sync(FULLMASK, se.x, bb);
             c_cnt = __shfl_sync(FULLMASK, se.y, bb);
             c_off = 0;
           }
-          const int take = min(filled - at, c_cnt - c_off);
-          if (lane == 0) stage_piece<FCH, LCH, GT>(stage[bi], &mbar[bi], ycur, G, at, c_start + c_off, take);
-          at += take;
+          const int take = min(CH - filled, c_cnt - c_off);
+          stage_piece<FCH, LCH, GT>(stage[bi], ycur, G, filled, c_start + c_off, take, lane);
+          filled += take;
           c_off += take;
         }
+        __syncwarp();   // the chunk is visible to every lane
         return filled;
       };
       int cur = 0;
       int nk = fill(cur);
       while (nk > 0) {
-        const int nk_next = fill(cur ^ 1);
-        const bool has_next = nk_next > 0;
-        const bool ok = __all_sync(FULLMASK, mbar_wait(&mbar[cur], parity[cur], kWaitLimit));
-        parity[cur] ^= 1u;
-        if (!ok) {
-          // a staged copy did not complete: record it, drain the other buffer, stop
-          if (lane == 0) atomicExch(B.err, CVO_ERR_TIMEOUT);
-          if (has_next) mbar_wait(&mbar[cur ^ 1], parity[cur ^ 1], kWaitLimit);
-          lost = true;
-          break;
-        }
         const Buf &sb = stage[cur];
         if (use_mma) {
           // candidate vectors of this chunk (lane k builds candidate k; empty slots are zero)
@@ -721,13 +684,13 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
             if (acc) { put(lane, cnt, __float_as_int(y.w), a); cnt++; }
           }
         }
-        __syncwarp();
-        nk = nk_next;
+        __syncwarp();   // every lane is done with the chunk before the next one is staged
         cur ^= 1;
+        nk = fill(cur);
       }
     }
   }
-  if (valid && !lost) finish_row(B, P, p, s, cnt, cap, ov);
+  if (valid) finish_row(B, P, p, s, cnt, cap, ov);
 }
 
 template <int FCH, int LCH, bool GT>
