@@ -497,6 +497,77 @@ def run_component(args):
                     "config": {"rows": rows, "cols": cols, "selected": 50000, "host_inputs": True},
                     "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "frames/s", "cores": 1, "kind": "port",
                                      "sample": "the whole frame (the oracle is single-threaded here)"}})
+    elif args.component == "adaptive":
+        from rkhs_ba_gb300 import AdaptiveCvoGPU
+        s, t, T_gt = scenes.room_pair(n=10000, seed=0)
+        p = CvoParams(params_path("geometric"))
+        cvo = AdaptiveCvoGPU(params=p)
+        res = {}
+
+        def reg():
+            res["r"] = cvo.align(s, t, np.eye(4))
+        sec = timed(reg)
+        ret, T, _, iters = res["r"]
+        rerr, terr = scenes.pose_error(T, T_gt)
+        # the oracle on a bounded sample: its first --cpu-iters iterations, scaled to the GPU's count
+        q = p.copy()
+        q.MAX_ITER = max(1, args.cpu_iters)
+        t0 = time.perf_counter()
+        orc.align_adaptive(q, s, t, np.eye(4))
+        per_iter = (time.perf_counter() - t0) / q.MAX_ITER
+        cpu_sec = per_iter * max(iters, 1)
+        out.update({"metric": "adaptive-ell registrations/s (10k-point room pair, geometric kernel)",
+                    "unit": "registrations/s", "value": round(1.0 / sec, 4), "ms_per_call": round(sec * 1000, 3),
+                    "iterations": int(iters), "ms_per_iteration": round(sec * 1000 / max(iters, 1), 3),
+                    "accuracy": {"rot_err_deg": round(rerr, 4), "trans_err_m": round(terr, 4)},
+                    "config": {"points": 10000, "params": "geometric.yaml", "kernel_matrices_per_iteration": 3,
+                               "cap": 512, "host_inputs": True},
+                    "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "registrations/s", "cores": cores,
+                                     "kind": "port", "sample": "%d oracle iterations scaled to the GPU's %d"
+                                                                % (q.MAX_ITER, iters)}})
+    elif args.component == "proposal":
+        from oracle import proposal as op
+        from rkhs_ba_gb300.proposal import ProposalNet, ScenePool
+        cvo = CvoGPU(params=CvoParams(params_path("color")))
+        pool = ScenePool(*ScenePool.generate(64, 2048, seed0=1_000_000))
+        net = ProposalNet(cvo, points_per_cloud=512, seed=0)
+        B, P = 64, 512
+        rng = np.random.default_rng(0)
+        batches = [(rng.integers(0, pool.n_scenes, size=B), np.stack([scenes.random_motion(rng) for _ in range(B)]),
+                    int(rng.integers(0, 2 ** 32))) for _ in range(args.warmup + args.steps)]
+        it = iter(batches)
+
+        def step():
+            sc, T, seed = next(it)
+            net.train_step(pool, sc, T, 1e-3, seed)
+        sec = timed(step)
+        pairs = make_pairs(args.pairs, args.points)
+        gs = [cvo.upload(a) for a, _, _ in pairs]
+        gt = [cvo.upload(b) for _, b, _ in pairs]
+        sec_inf = timed(lambda: net.hypotheses(gs, gt))
+        rows = 2 * B * P
+        enc = op.IN * op.H1 + op.H1 * op.H2
+        head = op.HEAD * op.H3 + op.H3 * op.OUT
+        # forward 2 m n k per product; backward: the input gradient and the weight gradient
+        # of every layer except the first layer's input gradient
+        fwd = 2.0 * (rows * enc + B * head)
+        bwd = 2.0 * (rows * (2 * enc - op.IN * op.H1) + 2 * B * head)
+        peak = None
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            with open(pk) as fh:
+                peak = float(json.load(fh)["bf16_tflops"])
+        tflops = (fwd + bwd) / sec / 1e12
+        out.update({"metric": "proposal training pairs/s (64 pairs x 2 clouds x 512 points per step)",
+                    "unit": "pairs/s", "value": round(B / sec, 2), "ms_per_step": round(sec * 1000, 3),
+                    "dtype": "bf16 operands, f32 accumulation",
+                    "inference_ms": round(sec_inf * 1000, 3),
+                    "inference_config": {"pairs": args.pairs, "points_per_cloud": args.points},
+                    "flops_per_step": fwd + bwd,
+                    "roofline": {"bound": "tensor", "achieved": round(tflops, 3), "peak": peak, "unit": "TFLOP/s",
+                                 "frac": round(tflops / peak, 6) if peak else None,
+                                 "note": "kernel launches and host synchronisation dominate: each product is small"},
+                    "config": {"batch": B, "points_per_cloud": P, "pool_scenes": 64}})
     print(json.dumps(out))
 
 
@@ -551,7 +622,7 @@ def main():
     ap.add_argument("--grid-steps", type=int, default=1, help="timed steps of the plain grid")
     ap.add_argument("--all24-pairs", type=int, default=2, help="pairs registered by the all-24 grid")
     ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
-    ap.add_argument("--component", default="", choices=["", "irls", "aniso", "frontend"],
+    ap.add_argument("--component", default="", choices=["", "irls", "aniso", "frontend", "proposal", "adaptive"],
                     help="time one component instead of the main workload")
     args = ap.parse_args()
     from rkhs_ba_gb300 import _build

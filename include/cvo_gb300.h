@@ -296,6 +296,25 @@ int cvo_register_hypotheses_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud
                                 int n_hyp, const float *T_init, float judge_ell,
                                 float T_out[16], int *best, float *cos_out, double *secs);
 
+/* ---------------------------------------------------- adaptive-ell CVO */
+/* AdaptiveCvoGPU::align(source, target, init_guess_transform, transform, seconds)
+ * (include/UnifiedCvo/cvo/AdaptiveCvoGPU.hpp:171-175, src/cvo/AdaptiveCvoGPU.cu:
+ * 1077-1250): CVO whose lengthscale follows the gradient of the inner product
+ * (ell <- ell - dl_step dl, backed off to 0.7 ell_max at ell_max, floor ell_min),
+ * with the three kernel matrices A, Axx, Ayy of fill_in_A_mat_gpu (:263-407: no
+ * range scaling, first 512 kept pairs per row in index order).  Same pose
+ * conventions as cvo_align; CVO_ZERO_GRADIENT for the reference's return -1. */
+int cvo_align_adaptive(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
+                       float T_out[16], double *secs, int *iters);
+/* Device clouds; trace (may be NULL) receives per iteration {ell, dl, step, nnz(A),
+ * nnz(Axx), nnz(Ayy)} for the first trace_len iterations. */
+int cvo_align_adaptive_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T_init[16],
+                           float T_out[16], double *secs, int *iters, double *trace, int trace_len);
+/* The kernel matrix A of the adaptive path at pose T and lengthscale ell
+ * (se_kernel -> fill_in_A_mat_gpu, src/cvo/AdaptiveCvoGPU.cu:263-443). */
+int cvo_compute_association_adaptive(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
+                                     const float T[16], float ell, cvo_assoc *out);
+
 /* ---------------------------------------------------- learned proposal */
 /* A point-set network that proposes K = 8 poses per pair for global registration,
  * standing in for the rotation grid of get_nearest_init_pose (src/cvo/CvoGPU.cpp:

@@ -651,6 +651,271 @@ int orc_align(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, c
   return ret;
 }
 
+/* ------------------------------------------------------- adaptive-ell CVO */
+/* AdaptiveCvoGPU (src/cvo/AdaptiveCvoGPU.cu).  Kernel matrices of
+ * fill_in_A_mat_gpu (:263-407): lengthscale ell without range scaling, the first
+ * ORC_ADAPTIVE_CAP kept pairs of every row in target index order, and its own
+ * thresholds and value formulas:
+ *   d2_thres   = -2 l l log(sp / s2)                  (double, rounded to float)
+ *   d2_c_thres = -2 c_ell c_ell log(sp / c_s / c_s)   (float quotient, double product)
+ *   geometric only:  a = s2 exp(-d2 / (2 l l)) c_sigma  (one double expression)
+ *   otherwise:       a = ck k sk, k = s2 exp(-d2/(2 l l)), ck = (c_s c_s) exp(-d2c/(2 c_ell c_ell)),
+ *                    sk = (s_s s_s) exp(-d2s/(2 s_ell s_ell)) with no semantic gate.
+ * The geometric-type factor does not exist on this path. */
+#define ORC_ADAPTIVE_CAP 512   /* KDTREE_K_SIZE, thirdparty/cugicp/cukdtree/cukdtree.h:12 */
+
+typedef struct {
+  float s2, sp, d2_c_thres;
+  int use_int, use_sem;
+} akconst;
+
+static akconst make_akconst(const cvo_params *p) {
+  akconst k;
+  k.s2 = p->sigma * p->sigma;
+  k.sp = p->sp_thres;
+  k.d2_c_thres = (float)(-2.0 * (double)p->c_ell * (double)p->c_ell *
+                         (double)logf(p->sp_thres / p->c_sigma / p->c_sigma));
+  k.use_int = p->is_using_intensity;
+  k.use_sem = p->is_using_semantics;
+  return k;
+}
+
+static float adaptive_d2_thres(const akconst *k, float l) {
+  return (float)(-2.0 * (double)l * (double)l * (double)logf(k->sp / k->s2));
+}
+
+/* Value of one pair (x from the rows' cloud, y from the columns'); 1 if kept. */
+static int pair_value_adaptive(const akconst *k, const cvo_params *p, const float *x, const float *fa,
+                               const float *la, const float *y, const float *fb, const float *lb, int F, int C,
+                               float l, float d2_thres, float *out) {
+  float d2 = sqdist3(y, x);
+  if (!(d2 < d2_thres)) return 0;
+  float a;
+  if (!k->use_int) {
+    a = (float)((double)k->s2 * exp(-(double)d2 / (2.0 * (double)l * (double)l)) * (double)p->c_sigma);
+  } else {
+    float d2c = sqdist_n(fa, fb, F);
+    if (!(d2c < k->d2_c_thres)) return 0;
+    float kk = (float)((double)k->s2 * exp(-(double)d2 / (2.0 * (double)l * (double)l)));
+    float ck = (float)((double)(p->c_sigma * p->c_sigma) *
+                       exp(-(double)d2c / (2.0 * (double)p->c_ell * (double)p->c_ell)));
+    float sk = 1.f;
+    if (k->use_sem) {
+      float d2s = sqdist_n(la, lb, C);
+      sk = (float)((double)(p->s_sigma * p->s_sigma) * exp(-(double)d2s / (2.0 * (double)p->s_ell * (double)p->s_ell)));
+    }
+    a = (ck * kk) * sk;
+  }
+  if (a > k->sp) { *out = a; return 1; }
+  return 0;
+}
+
+/* Kernel matrix rows (n rows of xs against the m points ys; F features, C labels
+ * per point, either may be 0) as ELL with stride ORC_ADAPTIVE_CAP. */
+int orc_fill_adaptive(const cvo_params *p, const float *xs, const float *fx, const float *lx, int n, const float *ys,
+                      const float *fy, const float *ly, int m, int F, int C, float ell, int *ind, float *val,
+                      int *nnz) {
+  const int cap = ORC_ADAPTIVE_CAP;
+  akconst k = make_akconst(p);
+  float d2t = adaptive_d2_thres(&k, ell);
+  grid_t g;
+  grid_build(&g, ys, m, sqrtf(d2t) * 1.001f + 1e-6f);
+  int fail = 0;
+#pragma omp parallel
+  {
+    int bufcap = m > 0 ? m : 1;
+    int *buf = (int *)malloc(sizeof(int) * (size_t)bufcap);
+    ja_t *kept = (ja_t *)malloc(sizeof(ja_t) * (size_t)bufcap);
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; i++) {
+      const float *x = xs + 3 * (size_t)i;
+      int nc = grid_candidates(&g, x, buf, bufcap);
+      if (nc > bufcap) { fail = 1; nc = bufcap; }
+      int nk = 0;
+      for (int t = 0; t < nc; t++) {
+        int j = buf[t];
+        float a;
+        if (pair_value_adaptive(&k, p, x, F ? fx + (size_t)i * F : NULL, C ? lx + (size_t)i * C : NULL,
+                                ys + 3 * (size_t)j, F ? fy + (size_t)j * F : NULL, C ? ly + (size_t)j * C : NULL, F,
+                                C, ell, d2t, &a)) {
+          kept[nk].j = j;
+          kept[nk].a = a;
+          nk++;
+        }
+      }
+      qsort(kept, (size_t)nk, sizeof(ja_t), cmp_ja);
+      int cnt = nk < cap ? nk : cap;
+      for (int t = 0; t < cnt; t++) {
+        ind[(size_t)i * cap + t] = kept[t].j;
+        val[(size_t)i * cap + t] = kept[t].a;
+      }
+      for (int t = cnt; t < cap; t++) { ind[(size_t)i * cap + t] = -1; val[(size_t)i * cap + t] = 0.f; }
+      nnz[i] = cnt;
+    }
+    free(buf);
+    free(kept);
+  }
+  grid_free(&g);
+  return fail ? -1 : 0;
+}
+
+/* Per-iteration trace of the adaptive loop (optional): ell used, dl, step, nnz of
+ * A / Axx / Ayy, the raw gradient. */
+typedef struct {
+  float *ell; double *dl; double *step; int64_t *nnz3; float *grad; int max_len;
+} orc_atrace;
+
+/* AdaptiveCvoGPU::align (src/cvo/AdaptiveCvoGPU.cu:1077-1250) with compute_flow
+ * (:548-891) and compute_step_size (:893-1075).  Sums in double.  Returns ret
+ * (-1: zero gradient); T_out = inverse of the internal pose (update_tf, :240-262). */
+int orc_align_adaptive(const cvo_params *p, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
+                       float T_out[16], int *iters_out, orc_atrace *trace) {
+  const int cap = ORC_ADAPTIVE_CAP;
+  int n = src->n, m = tgt->n, F = src->F, C = src->C;
+  if (n == 0 || m == 0) { if (iters_out) *iters_out = 0; return 0; }
+  float R[9], T[3];
+  for (int r = 0; r < 3; r++) {
+    for (int c = 0; c < 3; c++) R[3 * r + c] = T_init[c * 4 + r];
+    T[r] = T_init[12 + r];
+  }
+  float *xs = (float *)malloc(sizeof(float) * 3 * (size_t)(n ? n : 1));
+  for (int i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++) xs[3 * (size_t)i + d] = cloud_x(src, i, d);
+  float *ytr = (float *)malloc(sizeof(float) * 3 * (size_t)(m ? m : 1));
+  int *iA = (int *)malloc(sizeof(int) * (size_t)(n ? n : 1) * cap), *iX = (int *)malloc(sizeof(int) * (size_t)(n ? n : 1) * cap);
+  int *iY = (int *)malloc(sizeof(int) * (size_t)(m ? m : 1) * cap);
+  float *vA = (float *)malloc(sizeof(float) * (size_t)(n ? n : 1) * cap), *vX = (float *)malloc(sizeof(float) * (size_t)(n ? n : 1) * cap);
+  float *vY = (float *)malloc(sizeof(float) * (size_t)(m ? m : 1) * cap);
+  int *zA = (int *)malloc(sizeof(int) * (size_t)(n ? n : 1)), *zX = (int *)malloc(sizeof(int) * (size_t)(n ? n : 1));
+  int *zY = (int *)malloc(sizeof(int) * (size_t)(m ? m : 1));
+  float ell = p->ell_init, ell_max = p->ell_max;
+  int ret = 0, k = 0, iter = p->MAX_ITER;
+  for (; k < p->MAX_ITER; k++) {
+    float T44[16] = {0};
+    for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T44[c * 4 + r] = R[3 * r + c]; T44[12 + r] = T[r]; }
+    T44[15] = 1.f;
+    float Ri[9], Ti[3];
+    orc_pose_to_rinv(T44, Ri, Ti);
+    orc_transform(Ri, Ti, tgt, ytr);
+    orc_fill_adaptive(p, xs, src->features, src->labels, n, ytr, tgt->features, tgt->labels, m, F, C, ell, iA, vA, zA);
+    orc_fill_adaptive(p, xs, src->features, src->labels, n, xs, src->features, src->labels, n, F, C, ell, iX, vX, zX);
+    orc_fill_adaptive(p, ytr, tgt->features, tgt->labels, m, ytr, tgt->features, tgt->labels, m, F, C, ell, iY, vY, zY);
+    /* gradient and the lengthscale derivative */
+    double ell3 = (double)ell * (double)ell * (double)ell;
+    double g[6] = {0, 0, 0, 0, 0, 0}, dlA = 0.0, dlY = 0.0;
+    uint32_t nzA = 0, nzX = 0, nzY = 0;
+    for (int i = 0; i < n; i++) {
+      double x0 = xs[3 * i], x1 = xs[3 * i + 1], x2 = xs[3 * i + 2];
+      double w[3] = {0, 0, 0}, v[3] = {0, 0, 0}, dyx = 0.0, dxx = 0.0;
+      for (int t = 0; t < zA[i]; t++) {
+        int j = iA[(size_t)i * cap + t];
+        double a = vA[(size_t)i * cap + t];
+        double y0 = ytr[3 * j], y1 = ytr[3 * j + 1], y2 = ytr[3 * j + 2];
+        w[0] += a * (x1 * y2 - x2 * y1);
+        w[1] += a * (x2 * y0 - x0 * y2);
+        w[2] += a * (x0 * y1 - x1 * y0);
+        v[0] += a * (y0 - x0);
+        v[1] += a * (y1 - x1);
+        v[2] += a * (y2 - x2);
+        dyx -= a * ((y0 - x0) * (y0 - x0) + (y1 - x1) * (y1 - x1) + (y2 - x2) * (y2 - x2));
+      }
+      for (int t = 0; t < zX[i]; t++) {
+        int j = iX[(size_t)i * cap + t];
+        double a = vX[(size_t)i * cap + t];
+        double d0 = xs[3 * j] - x0, d1 = xs[3 * j + 1] - x1, d2 = xs[3 * j + 2] - x2;
+        dxx += a * (d0 * d0 + d1 * d1 + d2 * d2);
+      }
+      for (int t = 0; t < 3; t++) { g[t] += w[t] / (double)p->c; g[3 + t] += v[t] / (double)p->d; }
+      dlA += 2.0 / ell3 * dyx + 1.0 / ell3 * dxx;
+      nzA += (uint32_t)zA[i];
+      nzX += (uint32_t)zX[i];
+    }
+    for (int i = 0; i < m; i++) {
+      double s = 0.0;
+      for (int t = 0; t < zY[i]; t++) {
+        int j = iY[(size_t)i * cap + t];
+        double a = vY[(size_t)i * cap + t];
+        double d0 = ytr[3 * j] - ytr[3 * i], d1 = ytr[3 * j + 1] - ytr[3 * i + 1], d2 = ytr[3 * j + 2] - ytr[3 * i + 2];
+        s += a * (d0 * d0 + d1 * d1 + d2 * d2);
+      }
+      dlY += s / ell3;
+      nzY += (uint32_t)zY[i];
+    }
+    /* the reference's normaliser is unsigned arithmetic: Axx + Ayy - 2 A wraps */
+    uint32_t denom = nzX + nzY - 2u * nzA;
+    double dl = (double)((float)dlA + (float)dlY) / (double)denom;
+    float xi[6];
+    for (int t = 0; t < 6; t++) xi[t] = (float)g[t];
+    /* step size: the same Taylor terms as the two-view path at ell (no range scaling) */
+    cvo_params q = *p;
+    q.is_using_range_ell = 0;
+    double bcde[4];
+    orc_step_terms(&q, src, ytr, cap, iA, vA, zA, xi, ell, bcde);
+    /* coefficients rounded to float (Vector4f), smallest positive real root, else min_step; at most 0.8 */
+    double re[3], im[3], temp = DBL_MAX, step;
+    float c3 = (float)(4.0 * (double)(float)bcde[3]), c2 = (float)(3.0 * (double)(float)bcde[2]);
+    float c1 = (float)(2.0 * (double)(float)bcde[1]), c0 = (float)bcde[0];
+    if (orc_cubic_roots(c3, c2, c1, c0, re, im))
+      for (int t = 0; t < 3; t++)
+        if (re[t] > 0 && re[t] < temp && im[t] == 0.0) temp = re[t];
+    step = temp == DBL_MAX ? (double)p->min_step : temp;
+    if (step > 0.8) step = 0.8;
+    float stepf = (float)step;
+    if (trace && k < trace->max_len) {
+      if (trace->ell) trace->ell[k] = ell;
+      if (trace->dl) trace->dl[k] = dl;
+      if (trace->step) trace->step[k] = stepf;
+      if (trace->nnz3) { trace->nnz3[3 * k] = nzA; trace->nnz3[3 * k + 1] = nzX; trace->nnz3[3 * k + 2] = nzY; }
+      if (trace->grad) for (int t = 0; t < 6; t++) trace->grad[6 * k + t] = xi[t];
+    }
+    double wn = sqrt((double)xi[0] * xi[0] + (double)xi[1] * xi[1] + (double)xi[2] * xi[2]);
+    double vn = sqrt((double)xi[3] * xi[3] + (double)xi[4] * xi[4] + (double)xi[5] * xi[5]);
+    if (wn < p->eps && vn < p->eps) {
+      iter = k;
+      if (wn < 1e-8 && vn < 1e-8) ret = -1;
+      break;
+    }
+    float X[12];
+    orc_exp_sek3(xi, stepf, X);
+    float dRf[9], dTf[3], Tn[3], Rn[9];
+    for (int r = 0; r < 3; r++) {
+      for (int c = 0; c < 3; c++) dRf[3 * r + c] = X[4 * r + c];
+      dTf[r] = X[4 * r + 3];
+    }
+    /* float pose update, T = R dT + T, R = R dR */
+    for (int r = 0; r < 3; r++) Tn[r] = ((R[3 * r] * dTf[0] + R[3 * r + 1] * dTf[1]) + R[3 * r + 2] * dTf[2]) + T[r];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) Rn[3 * r + c] = (R[3 * r] * dRf[c] + R[3 * r + 1] * dRf[3 + c]) + R[3 * r + 2] * dRf[6 + c];
+    memcpy(R, Rn, sizeof(R));
+    memcpy(T, Tn, sizeof(T));
+    double dRd[9], dTd[3];
+    for (int t = 0; t < 9; t++) dRd[t] = dRf[t];
+    for (int t = 0; t < 3; t++) dTd[t] = dTf[t];
+    if (orc_dist_se3(dRd, dTd) < (double)p->eps_2) {
+      iter = k;
+      break;
+    }
+    /* lengthscale: gradient step, back-off at ell_max, floor at ell_min */
+    ell = (float)((double)ell - p->dl_step * dl);
+    if (ell >= ell_max) {
+      ell = (float)((double)ell_max * 0.7);
+      ell_max = (float)((double)ell_max * 0.7);
+    }
+    if (ell < p->ell_min) ell = p->ell_min;
+  }
+  if (iters_out) *iters_out = iter;
+  float T44[16] = {0};
+  for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T44[c * 4 + r] = R[3 * r + c]; T44[12 + r] = T[r]; }
+  T44[15] = 1.f;
+  float Ri[9], Ti[3];
+  orc_pose_to_rinv(T44, Ri, Ti);
+  memset(T_out, 0, sizeof(float) * 16);
+  for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) T_out[c * 4 + r] = Ri[3 * r + c]; T_out[12 + r] = Ti[r]; }
+  T_out[15] = 1.f;
+  free(xs); free(ytr); free(iA); free(iX); free(iY); free(vA); free(vX); free(vY); free(zA); free(zX); free(zY);
+  return ret;
+}
+
 /* --------------------------------------------------------- inner products */
 /* inner_product_impl (src/cvo/CvoGPU.cu:1673-1732): GPU semantics, cap =
  * nearest_neighbors_max, sum of the sparse matrix.  Also returns nnz. */

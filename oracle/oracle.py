@@ -53,6 +53,9 @@ def _lib():
             "orc_exp_sek3": (None, [fp, C.c_float, fp]),
             "orc_dist_se3": (C.c_double, [dp, dp]),
             "orc_align": (C.c_int, [vp, vp, vp, fp, fp, ip, vp]),
+            "orc_align_adaptive": (C.c_int, [vp, vp, vp, fp, fp, ip, vp]),
+            "orc_fill_adaptive": (C.c_int, [vp, fp, fp, fp, C.c_int, fp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                            ip, fp, ip]),
             "orc_inner_product_gpu": (C.c_double, [vp, vp, vp, fp, C.c_float, C.POINTER(C.c_int64)]),
             "orc_inner_product_cpu": (C.c_double, [vp, vp, vp, fp, C.c_float, C.POINTER(C.c_int64)]),
             "orc_function_angle": (C.c_double, [vp, vp, vp, fp, C.c_float, C.c_int, C.c_int]),
@@ -71,6 +74,14 @@ def _lib():
             f.restype = r
             f.argtypes = a
     return _L
+
+
+class OrcATrace(C.Structure):
+    _fields_ = [("ell", C.POINTER(C.c_float)), ("dl", C.POINTER(C.c_double)), ("step", C.POINTER(C.c_double)),
+                ("nnz3", C.POINTER(C.c_int64)), ("grad", C.POINTER(C.c_float)), ("max_len", C.c_int)]
+
+
+ADAPTIVE_CAP = 512
 
 
 class OrcTrace(C.Structure):
@@ -272,6 +283,47 @@ def align(params, src, tgt, T_init, trace_len: int = 0):
     ret = _lib().orc_align(_pp(params), _pc(s), _pc(t), Ti.ctypes.data_as(_fp), To.ctypes.data_as(_fp),
                            C.byref(iters), C.cast(C.byref(tr), C.c_void_p) if tr is not None else None)
     return ret, To.reshape(4, 4).T.copy(), iters.value, arrays
+
+
+def align_adaptive(params, src, tgt, T_init, trace_len: int = 0):
+    """AdaptiveCvoGPU::align restated on the CPU.  Returns (ret, T_out (4x4), iters, trace dict
+    with per-iteration ell, dl, step, nnz of A / Axx / Ayy and the raw gradient)."""
+    s, t = src.c_struct(), tgt.c_struct()
+    Ti = _m16(T_init)
+    To = np.zeros(16, np.float32)
+    iters = C.c_int(0)
+    tr = None
+    arrays = {}
+    if trace_len > 0:
+        arrays = dict(ell=np.zeros(trace_len, np.float32), dl=np.zeros(trace_len), step=np.zeros(trace_len),
+                      nnz3=np.zeros((trace_len, 3), np.int64), grad=np.zeros((trace_len, 6), np.float32))
+        dp = C.POINTER(C.c_double)
+        tr = OrcATrace(arrays["ell"].ctypes.data_as(_fp), arrays["dl"].ctypes.data_as(dp),
+                       arrays["step"].ctypes.data_as(dp), arrays["nnz3"].ctypes.data_as(C.POINTER(C.c_int64)),
+                       arrays["grad"].ctypes.data_as(_fp), trace_len)
+    ret = _lib().orc_align_adaptive(_pp(params), _pc(s), _pc(t), Ti.ctypes.data_as(_fp), To.ctypes.data_as(_fp),
+                                    C.byref(iters), C.cast(C.byref(tr), C.c_void_p) if tr is not None else None)
+    return ret, To.reshape(4, 4).T.copy(), iters.value, arrays
+
+
+def fill_adaptive(params, xs, fx, lx, ys, fy, ly, ell):
+    """Adaptive-path kernel matrix of rows xs (n, 3) against ys (m, 3) (features / labels
+    (n, F) / (n, C) or None): (ind (n, 512), val (n, 512), nnz (n,))."""
+    xs = np.ascontiguousarray(xs, np.float32)
+    ys = np.ascontiguousarray(ys, np.float32)
+    n, m = len(xs), len(ys)
+    F = 0 if fx is None else fx.shape[1]
+    Cn = 0 if lx is None else lx.shape[1]
+    f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+    fx, fy, lx, ly = f32(fx), f32(fy), f32(lx), f32(ly)
+    ptr = lambda a: a.ctypes.data_as(_fp) if a is not None else None
+    ind = np.zeros((max(n, 1), ADAPTIVE_CAP), np.int32)
+    val = np.zeros((max(n, 1), ADAPTIVE_CAP), np.float32)
+    nnz = np.zeros(max(n, 1), np.int32)
+    ip = C.POINTER(C.c_int)
+    _lib().orc_fill_adaptive(_pp(params), ptr(xs), ptr(fx), ptr(lx), n, ptr(ys), ptr(fy), ptr(ly), m, F, Cn,
+                             float(ell), ind.ctypes.data_as(ip), val.ctypes.data_as(_fp), nnz.ctypes.data_as(ip))
+    return ind[:n], val[:n], nnz[:n]
 
 
 def inner_product_gpu_semantics(params, src, tgt, T, ell):

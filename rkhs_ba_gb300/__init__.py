@@ -6,7 +6,7 @@ sm_103a) and bound through its C ABI (``include/cvo_gb300.h``).
 import os
 
 from .cloud import CvoPointCloud
-from .cvo import Association, CvoGPU, CvoParams, CvoResultInfo, GpuCloud
+from .cvo import AdaptiveCvoGPU, Association, CvoGPU, CvoParams, CvoResultInfo, GpuCloud
 
 PARAMS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "params")
 
@@ -16,4 +16,4 @@ def params_path(name: str) -> str:
     return os.path.join(PARAMS_DIR, name + ".yaml")
 
 
-__all__ = ["CvoPointCloud", "CvoGPU", "CvoParams", "CvoResultInfo", "Association", "GpuCloud", "params_path"]
+__all__ = ["CvoPointCloud", "CvoGPU", "AdaptiveCvoGPU", "CvoParams", "CvoResultInfo", "Association", "GpuCloud", "params_path"]

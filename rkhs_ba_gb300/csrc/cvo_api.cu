@@ -996,6 +996,57 @@ extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
   return CVO_OK;
 }
 
+// ----------------------------------------------------- adaptive-ell CVO
+extern "C" int cvo_align_adaptive_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T_init[16],
+                                      float T_out[16], double *secs, int *iters, double *trace, int trace_len) {
+  if (!H || !src || !tgt || !T_init || !T_out || trace_len < 0 || (trace_len > 0 && !trace)) return CVO_ERR_INVALID_ARG;
+  if (src->d->n == 0 || tgt->d->n == 0) {
+    if (iters) *iters = 0;
+    if (secs) *secs = 0;
+    return CVO_ERR_EMPTY_CLOUD;
+  }
+  return run_align_adaptive(&H->h, src->d, tgt->d, T_init, T_out, secs, iters, trace, trace_len);
+}
+
+extern "C" int cvo_align_adaptive(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
+                                  float T_out[16], double *secs, int *iters) {
+  if (!H || !src || !tgt || !T_init || !T_out) return CVO_ERR_INVALID_ARG;
+  if (src->n == 0 || tgt->n == 0) {
+    if (iters) *iters = 0;
+    if (secs) *secs = 0;
+    return CVO_ERR_EMPTY_CLOUD;
+  }
+  TmpClouds tc{H, {}};
+  cvo_gpu_cloud *s = nullptr, *t = nullptr;
+  int rc = cvo_cloud_upload(H, src, &s);
+  if (rc) return rc;
+  tc.v.push_back(s);
+  if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
+  tc.v.push_back(t);
+  return run_align_adaptive(&H->h, s->d, t->d, T_init, T_out, secs, iters, nullptr, 0);
+}
+
+extern "C" int cvo_compute_association_adaptive(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt,
+                                                const float T[16], float ell, cvo_assoc *out) {
+  if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
+  if (src->n == 0 || tgt->n == 0) {
+    fill_assoc(out, src->n, tgt->n, std::vector<int>((size_t)src->n + 1, 0), {}, {});
+    return CVO_OK;
+  }
+  TmpClouds tc{H, {}};
+  cvo_gpu_cloud *s = nullptr, *t = nullptr;
+  int rc = cvo_cloud_upload(H, src, &s);
+  if (rc) return rc;
+  tc.v.push_back(s);
+  if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
+  tc.v.push_back(t);
+  std::vector<int> rp, col;
+  std::vector<float> val;
+  if ((rc = run_association_adaptive(&H->h, s->d, t->d, T, ell, &rp, &col, &val))) return rc;
+  fill_assoc(out, src->n, tgt->n, rp, col, val);
+  return CVO_OK;
+}
+
 // ------------------------------------------------------ learned proposal
 struct cvo_proposal { NetDev *n; };
 

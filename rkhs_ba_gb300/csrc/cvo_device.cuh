@@ -126,8 +126,11 @@ constexpr float kBand = 2e-5f;      // relative band around sp_thres re-evaluate
 // so it is kept out of line to keep the hot loop's register count low.
 static __device__ __noinline__ float exact_value(const KParams &K, float l, float d2, float d2c, float d2s, float geo) {
   float kk = 1.f, ck = 1.f, sk = 1.f;
+  if (K.val_scale != 1.f && K.use_geo && !K.use_int && !K.use_sem)   // one double expression, rounded once
+    return __double2float_rn(dm(dm((double)K.sigma2, exp(__ddiv_rn(-(double)d2, dm(dm(2.0, (double)l), (double)l)))),
+                                (double)K.val_scale));
   if (K.use_geo) kk = __double2float_rn(dm((double)K.sigma2, exp(__ddiv_rn(-(double)d2, dm(dm(2.0, (double)l), (double)l)))));
-  if (K.use_int) ck = __double2float_rn(dm((double)K.c_sigma2, exp(__ddiv_rn(-(double)d2c, dm(2.0, (double)K.c2)))));
+  if (K.use_int) ck = __double2float_rn(dm((double)K.c_sigma2, exp(__ddiv_rn(-(double)d2c, K.two_c2))));
   if (K.use_sem)
     sk = __double2float_rn(dm((double)K.s_sigma_sq, exp(__ddiv_rn(-(double)d2s, dm(dm(2.0, (double)K.s_ell), (double)K.s_ell)))));
   return fm(fm(fm(ck, kk), sk), geo);

@@ -430,6 +430,8 @@ KParams make_kparams(const cvo_params &p) {
     float t = 2.f * k.c2;
     k.inv2c2 = 1.f / t;
   }
+  k.val_scale = 1.f;
+  k.two_c2 = 2.0 * (double)k.c2;
   // Kernel value bound: a <= sigma^2 c_sigma^2 s_sigma^2 exp(-(d2/(2l^2) + d2c/(2c^2))) (the geometric-type
   // factor is <= 1), so a > sp_thres needs the exponent below ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres).
   k.use_mma = 0;
@@ -439,6 +441,7 @@ KParams make_kparams(const cvo_params &p) {
     double lb = std::log((double)k.sigma2) - std::log((double)p.sp_thres);
     if (k.use_int) lb += std::log((double)k.c_sigma2);
     if (k.use_sem) lb += std::log((double)k.s_sigma_sq);
+    if (k.val_scale > 0.f) lb += std::log((double)k.val_scale);
     k.mma_tau = (float)(lb + 1e-3);
     k.use_mma = 1;
   }
@@ -917,11 +920,12 @@ int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::
 int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
                           const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
-                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out) {
+                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out,
+                          const KParams *kparams) {
   const int ne = (int)srcs.size();
   out->assign(ne, EdgeAssoc());
   if (ne == 0) return 0;
-  KParams K = make_kparams(h->params);
+  KParams K = kparams ? *kparams : make_kparams(h->params);
   std::vector<float> Tid(16 * (size_t)ne, 0.f);
   for (int e = 0; e < ne; e++) Tid[16 * e] = Tid[16 * e + 5] = Tid[16 * e + 10] = Tid[16 * e + 15] = 1.f;
   BatchHost bh;

@@ -82,6 +82,11 @@ struct KParams {
   // (mma_tau = ln(sigma^2 c_sigma^2 s_sigma^2 / sp_thres) + slack), see k_assoc.
   float mma_tau;
   int use_mma;
+  // Value scale (1 on the two-view path; c_sigma for the adaptive path's geometric-only
+  // values s^2 exp(-d2/2l^2) c_sigma) and the colour denominator 2 c_ell^2 of the exact
+  // (double) value as each path rounds it.
+  float val_scale;
+  double two_c2;
 };
 
 // Per-pair device state.  One struct per pair, in device memory.
@@ -244,13 +249,21 @@ struct EdgeAssoc {
 int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
                           const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
-                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out);
+                          const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out,
+                          const KParams *kparams = nullptr);
 
 // Non-isotropic association (cvo_aniso.cu): CSR of the kernel matrix with a 3x3
 // geometric kernel (column-major), first `cap` pairs per row in index order.
 void kernel_inverse3(const float K[9], float Ki[9]);
 int run_association_aniso(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], const float kernel[9],
                           int cap, std::vector<int> *rowptr, std::vector<int> *col, std::vector<float> *val);
+
+// Adaptive-lengthscale CVO (cvo_adaptive.cu).  trace (optional): per iteration
+// {ell, dl, step, nnz A, nnz Axx, nnz Ayy}.
+int run_association_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell,
+                             std::vector<int> *rowptr, std::vector<int> *col, std::vector<float> *val);
+int run_align_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const float T_init[16], float T_out[16],
+                       double *secs, int *iters_out, double *trace, int trace_len);
 
 // IRLS (cvo_irls.cu)
 int run_align_multi(Handle *h, int n_frames, DevCloud *const *clouds, double *poses, const uint8_t *hold_const,

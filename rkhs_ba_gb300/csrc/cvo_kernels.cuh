@@ -89,7 +89,7 @@ __device__ __forceinline__ bool eval_pair(const KParams &K, int F, int C, bool p
   float kf = K.use_geo ? fm(K.sigma2, __expf(fm(-d2, inv2l2))) : 1.f;
   float ckf = K.use_int ? fm(K.c_sigma2, __expf(fm(-d2c, K.inv2c2))) : 1.f;
   float skf = K.use_sem ? fm(K.s_sigma_sq, __expf(fm(-d2s, __frcp_rn(fm(fm(2.f, K.s_ell), K.s_ell))))) : 1.f;
-  float af = fm(fm(fm(ckf, kf), skf), geo);
+  float af = fm(fm(fm(fm(ckf, kf), skf), geo), K.val_scale);
   if (pass && fabsf(fs(af, K.sp_thres)) <= kBand * K.sp_thres) af = exact_value(K, l, d2, d2c, d2s, geo);
   a = af;
   return pass && (af > K.sp_thres);

@@ -648,12 +648,19 @@ int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *s
   // encoder: the max-pool routes dG to the pooled rows, then two ReLU layers
   CVO_CUDA_TRY(h, cudaMemsetAsync(n->dH2, 0, sizeof(float) * rows * kNetH2, h->stream));
   k_maxpool_bwd<<<(S * kNetH2 + 255) / 256, 256, 0, h->stream>>>(S, P, n->G, n->dG, n->arg, n->dH2);
-  const int split = (int)std::max<long long>(1, std::min<long long>(148, rows / 1024));
-  gemm(h, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2, split);
+  // split the row range of the weight gradients so that about 4 blocks per SM run,
+  // each over at least 64 rows
+  const int sms = h->num_sms > 0 ? h->num_sms : 152;
+  auto split_for = [&](int tiles) {
+    return (int)std::max<long long>(1, std::min<long long>((4LL * sms + tiles - 1) / tiles, rows / 64));
+  };
+  gemm(h, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2,
+       split_for(2));
   colsum(h, (int)rows, kNetH2, n->dH2, g + kOffB2);
   gemm(h, false, (int)rows, kNetH1, kNetH2, n->dH2, kNetH2, 1, w + kOffW2, 1, kNetH2, nullptr, n->dH1, kNetH1);
   k_relu_bwd<<<(unsigned)((rows * kNetH1 + 255) / 256), 256, 0, h->stream>>>(rows * kNetH1, n->H1, n->dH1);
-  gemm(h, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1, split);
+  gemm(h, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1,
+       split_for(1));
   colsum(h, (int)rows, kNetH1, n->dH1, g + kOffB1);
   h->launches += 3;
   if (lr > 0.f) {

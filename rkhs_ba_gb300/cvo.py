@@ -464,3 +464,45 @@ class CvoGPU:
                                      E.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs), C.byref(iters))
         L.check(rc, "cvo_align_multi", self._h)
         return P, secs.value, iters.value
+
+
+class AdaptiveCvoGPU(CvoGPU):
+    """cvo::AdaptiveCvoGPU (include/UnifiedCvo/cvo/AdaptiveCvoGPU.hpp:161-180): CVO whose
+    lengthscale follows the gradient of the inner product (src/cvo/AdaptiveCvoGPU.cu)."""
+
+    def align(self, source, target, T_init, trace_len: int = 0):
+        """int AdaptiveCvoGPU::align(src, tgt, init_guess_transform, transform&, secs*)
+        (:1077-1250).  Returns (ret, T_out, seconds, iters) and, with trace_len > 0, a
+        (iters, 6) trace {ell, dl, step, nnz A, nnz Axx, nnz Ayy} as a fifth value."""
+        T_out = np.zeros(16, np.float32)
+        secs = C.c_double(0)
+        iters = C.c_int(0)
+        Ti = _m16(T_init)
+        lib = L.lib()
+        tr = np.zeros((max(trace_len, 0), 6)) if trace_len > 0 else None
+        if isinstance(source, GpuCloud):
+            rc = lib.cvo_align_adaptive_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP),
+                                            T_out.ctypes.data_as(_FP), C.byref(secs), C.byref(iters),
+                                            tr.ctypes.data_as(C.POINTER(C.c_double)) if tr is not None else None,
+                                            int(max(trace_len, 0)))
+        else:
+            if tr is not None:
+                raise ValueError("a trace needs device clouds (upload them first)")
+            s, t = source.c_struct(), target.c_struct()
+            rc = lib.cvo_align_adaptive(self._h, C.byref(s), C.byref(t), Ti.ctypes.data_as(_FP),
+                                        T_out.ctypes.data_as(_FP), C.byref(secs), C.byref(iters))
+        L.check(rc, "cvo_align_adaptive", self._h)
+        out = ((0 if rc == L.CVO_OK else -1), _from16(T_out), secs.value, iters.value)
+        if tr is not None:
+            return out + (tr[:min(trace_len, iters.value + 1)],)
+        return out
+
+    def compute_association_gpu(self, source, target, T, ell) -> Association:
+        """The adaptive path's kernel matrix A at pose T and lengthscale ell
+        (se_kernel -> fill_in_A_mat_gpu, src/cvo/AdaptiveCvoGPU.cu:263-443)."""
+        ab = _AssocBuf()
+        s, t = source.c_struct(), target.c_struct()
+        L.check(L.lib().cvo_compute_association_adaptive(self._h, C.byref(s), C.byref(t), _m16(T).ctypes.data_as(_FP),
+                                                         float(ell), ab.h),
+                "cvo_compute_association_adaptive", self._h)
+        return _read_assoc(ab.h)
