@@ -315,6 +315,29 @@ int cvo_align_adaptive_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt
 int cvo_compute_association_adaptive(cvo_handle *h, const cvo_cloud *src, const cvo_cloud *tgt,
                                      const float T[16], float ell, cvo_assoc *out);
 
+/* ---------------------------------------------------------- pose graph */
+/* FP64 SE(3) pose graph for the reference's keyframe graph
+ * (src/graph_optimizer/PoseGraph.cpp:321-345 prior, :367-470 between factors,
+ * :471-495 GTSAM ISAM2 / fixed-lag update).  Poses are row-major 3x4 doubles
+ * [R | t], frame -> world; a between measurement is Xi^-1 Xj.  Errors follow GTSAM's
+ * PriorFactor / BetweenFactor<Pose3> (Log of the residual pose, rotation first),
+ * whitened by diagonal sigmas; cvo_pose_graph_optimize runs Levenberg-Marquardt to
+ * the batch optimum (ISAM2's estimate).  A graph needs at least one prior
+ * (CVO_ERR_UNSUPPORTED otherwise: the reference's GTSAM call throws on the
+ * indeterminate system). */
+typedef struct cvo_pose_graph cvo_pose_graph;
+int cvo_pose_graph_create(cvo_pose_graph **out);
+int cvo_pose_graph_destroy(cvo_pose_graph *g);
+/* initial (or new) value of a pose variable */
+int cvo_pose_graph_insert(cvo_pose_graph *g, int64_t key, const double pose[12]);
+int cvo_pose_graph_add_prior(cvo_pose_graph *g, int64_t key, const double pose[12], const double sigmas[6]);
+int cvo_pose_graph_add_between(cvo_pose_graph *g, int64_t from, int64_t to, const double rel[12],
+                               const double sigmas[6]);
+int cvo_pose_graph_optimize(cvo_pose_graph *g, int max_iters, double *initial_cost, double *final_cost, int *iters);
+int cvo_pose_graph_get(const cvo_pose_graph *g, int64_t key, double pose[12]);
+int cvo_pose_graph_size(const cvo_pose_graph *g, int *n_poses, int *n_factors);
+int cvo_pose_graph_cost(const cvo_pose_graph *g, double *cost);
+
 /* ---------------------------------------------------- learned proposal */
 /* A point-set network that proposes K = 8 poses per pair for global registration,
  * standing in for the rotation grid of get_nearest_init_pose (src/cvo/CvoGPU.cpp:

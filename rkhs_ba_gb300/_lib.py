@@ -103,6 +103,15 @@ SIGNATURES = {
     "cvo_align_adaptive": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _FP, _DP, _IP]),
     "cvo_align_adaptive_dev": (_i, [_P, _P, _P, _FP, _FP, _DP, _IP, _DP, _i]),
     "cvo_compute_association_adaptive": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _P]),
+    "cvo_pose_graph_create": (_i, [C.POINTER(_P)]),
+    "cvo_pose_graph_destroy": (_i, [_P]),
+    "cvo_pose_graph_insert": (_i, [_P, C.c_int64, _DP]),
+    "cvo_pose_graph_add_prior": (_i, [_P, C.c_int64, _DP, _DP]),
+    "cvo_pose_graph_add_between": (_i, [_P, C.c_int64, C.c_int64, _DP, _DP]),
+    "cvo_pose_graph_optimize": (_i, [_P, _i, _DP, _DP, _IP]),
+    "cvo_pose_graph_get": (_i, [_P, C.c_int64, _DP]),
+    "cvo_pose_graph_size": (_i, [_P, _IP, _IP]),
+    "cvo_pose_graph_cost": (_i, [_P, _DP]),
     "cvo_proposal_create": (_i, [_P, _i, C.c_uint32, C.POINTER(_P)]),
     "cvo_proposal_destroy": (_i, [_P]),
     "cvo_proposal_dims": (_i, [_P, _IP, _IP, _IP]),
