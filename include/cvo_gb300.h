@@ -376,12 +376,14 @@ int cvo_proposal_hypotheses_dev(cvo_handle *h, cvo_proposal *p, int n_pairs, cvo
  * at rank_ell, the best n_refine (1..8) of each pair refined by one batched align
  * and judged by the final cos-angle at judge_ell; pairs judged below fallback_cos
  * are registered again from the 24-rotation grid and keep the better result.
+ * refine_ell > 0 starts the hypotheses' refinement at that lengthscale instead of
+ * ell_init (the grid fallback keeps ell_init).
  * T_out: n_pairs x 16 (cvo_align's T_out convention); cos_out, used_fallback and
  * iters (align iterations summed over the pair's refinements) may be NULL. */
 int cvo_register_learned_batch_dev(cvo_handle *h, cvo_proposal *p, int n_pairs, cvo_gpu_cloud *const *srcs,
                                    cvo_gpu_cloud *const *tgts, int n_refine, float rank_ell, float judge_ell,
-                                   float fallback_cos, uint32_t seed, float *T_out, float *cos_out,
-                                   int *used_fallback, int *iters, double *secs);
+                                   float fallback_cos, float refine_ell, uint32_t seed, float *T_out,
+                                   float *cos_out, int *used_fallback, int *iters, double *secs);
 
 /* ---------------------------------------------------------- multi-frame */
 /* CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670)

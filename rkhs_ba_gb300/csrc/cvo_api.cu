@@ -1126,9 +1126,9 @@ extern "C" int cvo_proposal_hypotheses_dev(cvo_handle *H, cvo_proposal *p, int n
 // the two.
 extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, int n_pairs,
                                               cvo_gpu_cloud *const *srcs, cvo_gpu_cloud *const *tgts, int n_refine,
-                                              float rank_ell, float judge_ell, float fallback_cos, uint32_t seed,
-                                              float *T_out, float *cos_out, int *used_fallback, int *iters,
-                                              double *secs) {
+                                              float rank_ell, float judge_ell, float fallback_cos, float refine_ell,
+                                              uint32_t seed, float *T_out, float *cos_out, int *used_fallback,
+                                              int *iters, double *secs) {
   constexpr int kHyp = 8;
   if (!H || !p || n_pairs <= 0 || !srcs || !tgts || !T_out || n_refine < 1 || n_refine > kHyp)
     return CVO_ERR_INVALID_ARG;
@@ -1198,7 +1198,14 @@ extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, in
     }
   std::vector<float> Tr, cv;
   std::vector<int> it;
-  if ((rc = refine_and_judge(owner, inits, &Tr, &cv, &it))) return rc;
+  {
+    // the hypotheses' refinement may start at a finer lengthscale than a grid start
+    const float ell0 = h->params.ell_init;
+    if (refine_ell > 0.f) h->params.ell_init = refine_ell;
+    rc = refine_and_judge(owner, inits, &Tr, &cv, &it);
+    h->params.ell_init = ell0;
+    if (rc) return rc;
+  }
   std::vector<float> best_cos(n_pairs, -INFINITY);
   std::vector<int> total_it(n_pairs, 0);
   for (size_t q = 0; q < owner.size(); q++) {

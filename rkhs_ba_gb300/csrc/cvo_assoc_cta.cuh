@@ -297,7 +297,7 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
 // Persistent blocks take work items (four tiles each) from a counter, so blocks
 // that finish early pick up the remaining tiles.
 template <int FCH, int LCH, bool GT>
-__global__ void __launch_bounds__(kCtaRows) k_assoc_cta(BatchDev B, KParams K) {
+__global__ void __launch_bounds__(kCtaRows, 4) k_assoc_cta(BatchDev B, KParams K) {
   extern __shared__ __align__(128) unsigned char cta_smem[];
   __shared__ int item;
   const int items = B.total_warps / kCtaWarps;

@@ -416,10 +416,12 @@ class CvoGPU:
         return _from16(To), best.value, cos, secs.value
 
     def register_learned_batch(self, net, sources, targets, n_refine: int = 2, rank_ell: float | None = None,
-                               judge_ell: float | None = None, fallback_cos: float = 0.0, seed: int = 0):
+                               judge_ell: float | None = None, fallback_cos: float = 0.0, seed: int = 0,
+                               refine_ell: float = 0.0):
         """Global registration of many pairs from the proposal network's hypotheses
         (ranked, best n_refine refined in one batch, judged by the final cos-angle,
-        24-rotation grid fallback below fallback_cos).  Returns (T_out list of 4x4 in
+        24-rotation grid fallback below fallback_cos; refine_ell > 0 starts the refinement
+        at that lengthscale).  Returns (T_out list of 4x4 in
         align's output convention, cos (B,), used_fallback (B,), iters (B,), seconds)."""
         p = self.get_params()
         rank_ell = p.ell_init_first_frame if rank_ell is None else rank_ell
@@ -433,7 +435,7 @@ class CvoGPU:
         its = np.zeros(n, np.int32)
         secs = C.c_double(0)
         L.check(L.lib().cvo_register_learned_batch_dev(self._h, net.handle, n, S, Tg, int(n_refine), float(rank_ell),
-                                                       float(judge_ell), float(fallback_cos),
+                                                       float(judge_ell), float(fallback_cos), float(refine_ell),
                                                        C.c_uint32(seed & 0xFFFFFFFF), To.ctypes.data_as(_FP),
                                                        cos.ctypes.data_as(_FP),
                                                        fb.ctypes.data_as(C.POINTER(C.c_int)),

@@ -100,7 +100,7 @@ class PoseGraph:
     """cvo::PoseGraph(is_f2f, optimizer, num_frames_in_window) with the GB300 CVO as its tracker."""
 
     def __init__(self, cvo, is_f2f: bool = True, keyframe_threshold: float = 0.5, loop_quality: float = 0.6,
-                 loop_accept: float = 0.0, ell: float | None = None, first_pose=None):
+                 loop_accept: float = 0.0, ell: float | None = None, first_pose=None, first_motion_guess=None):
         self.cvo = cvo
         self.is_f2f = is_f2f
         self.keyframe_threshold = keyframe_threshold
@@ -108,6 +108,8 @@ class PoseGraph:
         self.loop_accept = loop_accept
         self.ell = cvo.get_params().ell_init if ell is None else ell
         self.first_pose = np.eye(4) if first_pose is None else np.asarray(first_pose, float)
+        # the first pair's initial guess (the reference reads it from a file, read_tracking_init_guess, :54-72)
+        self.first_motion_guess = np.eye(4) if first_motion_guess is None else np.asarray(first_motion_guess, float)
         self.solver = PoseGraphSolver()
         self.clouds = {}           # frame id -> device cloud
         self.ref = {}              # frame id -> (reference keyframe id, ref -> frame)
@@ -162,7 +164,7 @@ class PoseGraph:
             slast = self.order[-2]
             v = _inv(self.compute_frame_pose_in_graph(slast)) @ self.compute_frame_pose_in_graph(last)
         else:
-            v = np.eye(4)
+            v = self.first_motion_guess
         if self.is_f2f:
             rel = self._align(last, fid, v)
             kf_to_new = _inv(self.kf_pose[last_kf]) @ self.compute_frame_pose_in_graph(last) @ rel
