@@ -186,7 +186,7 @@ def run_ours(args):
 
     def register_learned(gs, gt):
         Ts, cos, fb, its, _ = cvo.register_learned_batch(net, gs, gt, n_refine=args.refine,
-                                                         fallback_cos=args.fallback_cos)
+                                                         fallback_cos=args.fallback_cos, refine_ell=args.refine_ell)
         return Ts, its, fb
 
     def register_grid(gs, gt):
@@ -338,6 +338,7 @@ def run_ours(args):
                                "24-rotation grid fallback" % args.refine,
                    "points_per_cloud": args.points, "pairs_per_step": args.pairs, "params": "color.yaml",
                    "rotation": "uniform SO(3)", "translation_max_m": 2.0, "fallback_cos": args.fallback_cos,
+                   "refine_ell": args.refine_ell,
                    "l2": "256 MB buffer written between timed steps", "parallelism": "replicas"},
         "accuracy": {"success_rate": float(np.mean(succ)), "criterion": "rot<2deg, trans<5cm",
                      "mean_iters": float(np.mean(its)), "fallbacks": int(np.sum(fb))},
@@ -613,6 +614,8 @@ def main():
     ap.add_argument("--ref-iters", type=float, default=251.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refine", type=int, default=1, help="hypotheses refined per pair (1..8)")
+    ap.add_argument("--refine-ell", type=float, default=0.4,
+                    help="lengthscale the hypotheses' refinement starts at (0: ell_init of the yaml)")
     ap.add_argument("--fallback-cos", type=float, default=0.0,
                     help="judged cos-angle below which a pair falls back to the grid")
     ap.add_argument("--train-scenes", type=int, default=600)
