@@ -212,6 +212,15 @@ def run_ours(args):
 
     gs = [cvo.upload(s) for s, _, _ in pairs]
     gt = [cvo.upload(t) for _, t, _ in pairs]
+    # association cell size picked by the autotuner on the first pair (untimed setup)
+    tune = None
+    if not args.no_autotune:
+        # at the pose and lengthscale the refinement starts from: the network's first hypothesis
+        hyp0 = net.hypotheses([gs[0]], [gt[0]])[0, 0]
+        r = cvo.autotune(gs[0], gt[0], hyp0, ell=args.refine_ell if args.refine_ell > 0 else p.ell_init, reps=2)
+        b = r["configs"][r["best"]]
+        tune = {"div_r": b[0], "div_ext": b[1], "ms": round(b[2], 3),
+                "default_ms": round(next(ms for a, e, ms in r["configs"] if (a, e) == (4.0, 8.0)), 3)}
 
     for _ in range(args.warmup):
         register_learned(gs, gt)
@@ -347,6 +356,7 @@ def run_ours(args):
                        "note": "nearest of the 24 grid rotations by cos-angle, then one batched align"},
         "plain_grid_all24": all24,
         "proposal": prop_info,
+        "autotune": tune,
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -614,6 +624,7 @@ def main():
     ap.add_argument("--ref-iters", type=float, default=251.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refine", type=int, default=1, help="hypotheses refined per pair (1..8)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default association cell size")
     ap.add_argument("--refine-ell", type=float, default=0.4,
                     help="lengthscale the hypotheses' refinement starts at (0: ell_init of the yaml)")
     ap.add_argument("--fallback-cos", type=float, default=0.0,

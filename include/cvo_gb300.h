@@ -296,6 +296,24 @@ int cvo_register_hypotheses_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud
                                 int n_hyp, const float *T_init, float judge_ell,
                                 float T_out[16], int *best, float *cos_out, double *secs);
 
+/* ------------------------------------------------------------ autotuner */
+/* The association's grid cell size for search radius r and source tiles of diagonal
+ * ext is max(r / div_r, (ext + 2 r) / div_ext).  cvo_autotune_dev times one
+ * association pass of (src, tgt) at pose T and lengthscale ell (<= 0: ell_init) for
+ * each candidate (div_r in {2, 3, 4, 6} x div_ext in {4, 8, 16}; median of reps) and
+ * keeps the fastest for every later batch with the same (F, C, log2 rows) key.  The
+ * kernel matrix does not depend on the choice (kept pairs are defined by index order);
+ * only the candidate work per row does.  Arrays (max_configs entries, may be NULL)
+ * receive every candidate and its time in ms; best its index.  No reference
+ * counterpart: the reference's block size and kd-tree are compile-time choices
+ * (CMakeLists.txt:473-558, src/experiments/cuda_performance_tune.cu:3-45). */
+int cvo_autotune_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell, int reps,
+                     int max_configs, int *n_configs, float *div_r, float *div_ext, float *ms, int *best);
+/* Set / read the configuration of a key (for a cache the caller persists); get returns
+ * CVO_ERR_INVALID_ARG and the defaults (4, 8) for a key that was never tuned. */
+int cvo_tune_set(cvo_handle *h, int F, int C, int64_t rows, float div_r, float div_ext);
+int cvo_tune_get(const cvo_handle *h, int F, int C, int64_t rows, float *div_r, float *div_ext);
+
 /* ---------------------------------------------------- adaptive-ell CVO */
 /* AdaptiveCvoGPU::align(source, target, init_guess_transform, transform, seconds)
  * (include/UnifiedCvo/cvo/AdaptiveCvoGPU.hpp:171-175, src/cvo/AdaptiveCvoGPU.cu:

@@ -100,6 +100,9 @@ SIGNATURES = {
     "cvo_get_nearest_init_pose_dev": (_i, [_P, _P, _P, _f, _i, _i, _FP, _DP]),
     "cvo_rotation_grid": (_i, [_i, _i, _FP, _i]),
     "cvo_register_hypotheses_dev": (_i, [_P, _P, _P, _i, _FP, _f, _FP, _IP, _FP, _DP]),
+    "cvo_autotune_dev": (_i, [_P, _P, _P, _FP, _f, _i, _i, _IP, _FP, _FP, _FP, _IP]),
+    "cvo_tune_set": (_i, [_P, _i, _i, C.c_int64, _f, _f]),
+    "cvo_tune_get": (_i, [_P, _i, _i, C.c_int64, _FP, _FP]),
     "cvo_align_adaptive": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _FP, _DP, _IP]),
     "cvo_align_adaptive_dev": (_i, [_P, _P, _P, _FP, _FP, _DP, _IP, _DP, _i]),
     "cvo_compute_association_adaptive": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f, _P]),

@@ -996,6 +996,46 @@ extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
   return CVO_OK;
 }
 
+// ------------------------------------------------------------ autotuner
+extern "C" int cvo_autotune_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell,
+                                int reps, int max_configs, int *n_configs, float *div_r, float *div_ext, float *ms,
+                                int *best) {
+  if (!H || !src || !tgt || !T || max_configs < 0) return CVO_ERR_INVALID_ARG;
+  if (!(ell > 0.f)) ell = H->h.params.ell_init;
+  std::vector<TuneConfig> cfg;
+  std::vector<float> t;
+  int bi = 0;
+  int rc = autotune_association(&H->h, src->d, tgt->d, T, ell, reps, &cfg, &t, &bi);
+  if (rc) return rc;
+  if (n_configs) *n_configs = (int)cfg.size();
+  for (int k = 0; k < (int)cfg.size() && k < max_configs; k++) {
+    if (div_r) div_r[k] = cfg[k].cell_div_r;
+    if (div_ext) div_ext[k] = cfg[k].cell_div_ext;
+    if (ms) ms[k] = t[k];
+  }
+  if (best) *best = bi;
+  return CVO_OK;
+}
+
+extern "C" int cvo_tune_set(cvo_handle *H, int F, int C, int64_t rows, float div_r, float div_ext) {
+  if (!H || F < 0 || C < 0 || rows < 0 || !(div_r > 0.f) || !(div_ext > 0.f)) return CVO_ERR_INVALID_ARG;
+  TuneConfig c;
+  c.cell_div_r = div_r;
+  c.cell_div_ext = div_ext;
+  H->h.tuned[tune_key(F, C, rows)] = c;
+  return CVO_OK;
+}
+
+extern "C" int cvo_tune_get(const cvo_handle *H, int F, int C, int64_t rows, float *div_r, float *div_ext) {
+  if (!H || !div_r || !div_ext) return CVO_ERR_INVALID_ARG;
+  TuneConfig c;
+  auto it = H->h.tuned.find(tune_key(F, C, rows));
+  if (it != H->h.tuned.end()) c = it->second;
+  *div_r = c.cell_div_r;
+  *div_ext = c.cell_div_ext;
+  return it != H->h.tuned.end() ? CVO_OK : CVO_ERR_INVALID_ARG;
+}
+
 // ----------------------------------------------------- adaptive-ell CVO
 extern "C" int cvo_align_adaptive_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T_init[16],
                                       float T_out[16], double *secs, int *iters, double *trace, int trace_len) {

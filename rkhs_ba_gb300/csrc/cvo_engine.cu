@@ -451,9 +451,19 @@ KParams make_kparams(const cvo_params &p) {
 // Cell size for search radius r and source tiles of diagonal ext: small against r
 // (the distance test on cells then trims the query box towards the union of balls)
 // while keeping a tile's box at about 8 cells per axis.
-static float cell_for_radius(float r, float ext) { return std::max(0.25f * r, 0.125f * (ext + 2.f * r)); }
+static float cell_for_radius(float r, float ext, const TuneConfig &c) {
+  return std::max(r / c.cell_div_r, (ext + 2.f * r) / c.cell_div_ext);
+}
 // Largest radius a cell of size hc serves (inverse of cell_for_radius).
-static float radius_for_cell(float hc, float ext) { return std::max(0.f, std::min(4.f * hc, 0.5f * (8.f * hc - ext))); }
+static float radius_for_cell(float hc, float ext, const TuneConfig &c) {
+  return std::max(0.f, std::min(c.cell_div_r * hc, 0.5f * (c.cell_div_ext * hc - ext)));
+}
+
+long long tune_key(int F, int C, long long rows) {
+  int b = 0;
+  while ((1LL << (b + 1)) <= rows && b < 40) b++;
+  return ((long long)F << 32) | ((long long)C << 16) | b;
+}
 
 static float host_range_ell(float ell, float dist) { return (float)(((double)dist / 500.0 + 1.0) * (double)ell); }
 static float host_radius(const KParams &K, float ell, float norm) {
@@ -491,6 +501,16 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   }
   int rc = select_kernels(K, F, C, bh->assoc, bh->rescan, bh->assoc_smem, bh->assoc_per_sm);
   if (rc) return rc;
+  // cell-size configuration: forced by the autotuner, else the tuned one for this key, else the default
+  TuneConfig tc;
+  if (h->tune_force) {
+    tc = *h->tune_force;
+  } else {
+    long long maxn = 0;
+    for (int p = 0; p < np; p++) maxn = std::max<long long>(maxn, srcs[p]->n);
+    auto it = h->tuned.find(tune_key(F, C, maxn));
+    if (it != h->tuned.end()) tc = it->second;
+  }
   // grid levels per pair
   std::vector<std::vector<GridDesc>> lv(np);
   std::vector<std::vector<float>> lr(np);
@@ -505,7 +525,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
       float ell_lo = (mode == MODE_ALIGN) ? std::min(K.ell_min, ell_hi) : ell_hi;
       float r_hi = host_radius(K, ell_hi, srcs[p]->max_norm);
       float r_lo = host_radius(K, ell_lo, 0.f);
-      int e_hi = level_for_radius(cell_for_radius(r_hi, ext)), e_lo = level_for_radius(cell_for_radius(r_lo, ext));
+      int e_hi = level_for_radius(cell_for_radius(r_hi, ext, tc)), e_lo = level_for_radius(cell_for_radius(r_lo, ext, tc));
       if (e_hi - e_lo + 1 > 24) e_lo = e_hi - 23;
       for (int e = e_lo; e <= e_hi; e++) exps.push_back(e);
     }
@@ -513,7 +533,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
       GridDesc g;
       if ((rc = cloud_level(h, t, e, &g))) return rc;
       lv[p].push_back(g);
-      lr[p].push_back(e >= 1000 ? INFINITY : radius_for_cell(g.h, ext));
+      lr[p].push_back(e >= 1000 ? INFINITY : radius_for_cell(g.h, ext, tc));
     }
   }
   // sizes
@@ -894,6 +914,57 @@ int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, cons
   if ((rc = read_pairs(h, &bh))) return rc;
   for (int p = 0; p < np; p++) (*asum)[p] = bh.pairs[p].asum;
   return 0;
+}
+
+int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell, int reps,
+                         std::vector<TuneConfig> *configs, std::vector<float> *ms, int *best) {
+  // candidates: cells of r/2 .. r/6 against the radius, tile-box terms of 4 .. 16 cells
+  const float div_r[] = {2.f, 3.f, 4.f, 6.f};
+  const float div_ext[] = {4.f, 8.f, 16.f};
+  configs->clear();
+  for (float a : div_r)
+    for (float b : div_ext) {
+      TuneConfig c;
+      c.cell_div_r = a;
+      c.cell_div_ext = b;
+      configs->push_back(c);
+    }
+  ms->assign(configs->size(), INFINITY);
+  if (src->n == 0 || tgt->n == 0) return CVO_ERR_EMPTY_CLOUD;
+  reps = std::max(1, reps);
+  std::vector<float> Tv(T, T + 16);
+  const int cap = h->params.nearest_neighbors_max;
+  cudaEvent_t e0, e1;
+  CVO_CUDA_TRY(h, cudaEventCreate(&e0));
+  CVO_CUDA_TRY(h, cudaEventCreate(&e1));
+  int rc = 0, bi = 0;
+  for (size_t k = 0; k < configs->size() && !rc; k++) {
+    h->tune_force = &(*configs)[k];
+    std::vector<double> asum;
+    rc = run_inner_product_pairs(h, {src}, {tgt}, Tv, ell, cap, &asum);   // builds this configuration's levels
+    std::vector<float> t;
+    for (int r = 0; r < reps && !rc; r++) {
+      cudaEventRecord(e0, h->stream);
+      rc = run_inner_product_pairs(h, {src}, {tgt}, Tv, ell, cap, &asum);
+      cudaEventRecord(e1, h->stream);
+      cudaEventSynchronize(e1);
+      float dt = 0.f;
+      cudaEventElapsedTime(&dt, e0, e1);
+      t.push_back(dt);
+    }
+    if (!rc) {
+      std::sort(t.begin(), t.end());
+      (*ms)[k] = t[t.size() / 2];
+      if ((*ms)[k] < (*ms)[bi]) bi = (int)k;
+    }
+  }
+  h->tune_force = nullptr;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  h->tuned[tune_key(src->F, src->C, src->n)] = (*configs)[bi];
+  if (best) *best = bi;
+  return CVO_OK;
 }
 
 int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::vector<float> &T, float ell, int cap,

@@ -174,6 +174,14 @@ struct Profile {
   long long iterations = 0;
 };
 
+// Association tuning: grid cell size h = max(r / cell_div_r, (ext + 2 r) / cell_div_ext)
+// for search radius r and source tiles of diagonal ext.  Results do not depend on it
+// (the kept pairs are defined by index order), only the work per row does.
+struct TuneConfig {
+  float cell_div_r = 4.f;
+  float cell_div_ext = 8.f;
+};
+
 struct Handle {
   cvo_params params;
   cudaStream_t stream = nullptr;
@@ -184,7 +192,15 @@ struct Handle {
   long long launches = 0;
   std::string last_error;
   Workspace *ws = nullptr;
+  std::map<long long, TuneConfig> tuned;    // (F, C, log2 rows) -> fastest configuration
+  const TuneConfig *tune_force = nullptr;   // set while the autotuner times a configuration
 };
+
+long long tune_key(int F, int C, long long rows);
+// Times one association pass of (src, tgt) at pose T and lengthscale ell for every
+// candidate configuration and records the fastest for the batches that match its key.
+int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell, int reps,
+                         std::vector<TuneConfig> *configs, std::vector<float> *ms, int *best);
 
 // Label rows are padded to 5 float4 chunks (C <= 20) or 9 chunks (C <= 36).
 inline int label_chunks(int C) { return C <= 0 ? 0 : (C <= 20 ? 5 : (C <= 36 ? 9 : (C + 3) / 4)); }

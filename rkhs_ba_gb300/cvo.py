@@ -443,6 +443,29 @@ class CvoGPU:
                 "cvo_register_learned_batch_dev", self._h)
         return [_from16(To[16 * i:16 * i + 16]) for i in range(n)], cos, fb, its, secs.value
 
+    # -- autotuner -----------------------------------------------------
+    def autotune(self, source: GpuCloud, target: GpuCloud, T=None, ell: float = 0.0, reps: int = 3) -> dict:
+        """Times the association's cell-size configurations on one pair and keeps the fastest
+        for later batches of the same (F, C, size) key.  Returns {"configs": [(div_r, div_ext,
+        ms), ...], "best": index}."""
+        Ti = _m16(np.eye(4) if T is None else T)
+        n = C.c_int()
+        dr, de, ms = np.zeros(16, np.float32), np.zeros(16, np.float32), np.zeros(16, np.float32)
+        best = C.c_int()
+        L.check(L.lib().cvo_autotune_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP), float(ell),
+                                         int(reps), 16, C.byref(n), dr.ctypes.data_as(_FP), de.ctypes.data_as(_FP),
+                                         ms.ctypes.data_as(_FP), C.byref(best)), "cvo_autotune_dev", self._h)
+        return {"configs": [(float(dr[k]), float(de[k]), float(ms[k])) for k in range(n.value)], "best": best.value}
+
+    def tune_set(self, F: int, Cn: int, rows: int, div_r: float, div_ext: float) -> None:
+        L.check(L.lib().cvo_tune_set(self._h, F, Cn, rows, float(div_r), float(div_ext)), "cvo_tune_set", self._h)
+
+    def tune_get(self, F: int, Cn: int, rows: int):
+        """(div_r, div_ext, tuned?) for a key."""
+        a, b = C.c_float(), C.c_float()
+        rc = L.lib().cvo_tune_get(self._h, F, Cn, rows, C.byref(a), C.byref(b))
+        return a.value, b.value, rc == 0
+
     # -- multi-frame ----------------------------------------------------
     def align_multi(self, clouds, poses, hold_const, edges):
         """CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670).
