@@ -301,13 +301,48 @@ __global__ void __launch_bounds__(kCtaRows, 4) k_assoc_cta(BatchDev B, KParams K
   extern __shared__ __align__(128) unsigned char cta_smem[];
   __shared__ int item;
   const int items = B.total_warps / kCtaWarps;
+  int last = -1;
+  long long t0 = 0;
   while (true) {
-    __syncthreads();   // every thread has read the previous item; shared memory is free
-    if (threadIdx.x == 0) item = atomicAdd(B.assoc_next, 1);
+    __syncthreads();   // every thread has finished the previous item; shared memory is free
+    if (threadIdx.x == 0) {
+      if (last >= 0) B.item_cost[last] = (int)min((clock64() - t0) >> 8, 0x7FFFFFFFLL);
+      item = atomicAdd(B.assoc_next, 1);
+    }
     __syncthreads();
     const int it = item;
     if (it >= items) break;
-    assoc_block<FCH, LCH, GT>(B, K, it * kCtaWarps, cta_smem);
+    const int wi = B.item_order[it];
+    if (threadIdx.x == 0) {
+      last = wi;
+      t0 = clock64();
+    }
+    assoc_block<FCH, LCH, GT>(B, K, wi * kCtaWarps, cta_smem);
+  }
+}
+
+// Orders the work items for the next pass: descending buckets of log2 cost (one block;
+// the order inside a bucket is arbitrary and does not change any result).
+__global__ void __launch_bounds__(1024) k_order_items(int n, const int *cost, int *order) {
+  __shared__ int hist[33], off[33];
+  for (int b = threadIdx.x; b < 33; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int c = cost[i];
+    atomicAdd(&hist[c > 0 ? 32 - __clz(c) : 0], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int b = 32; b >= 0; b--) {
+      off[b] = run;
+      run += hist[b];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int c = cost[i];
+    order[atomicAdd(&off[c > 0 ? 32 - __clz(c) : 0], 1)] = i;
   }
 }
 

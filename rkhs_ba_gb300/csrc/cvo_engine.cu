@@ -579,6 +579,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   add(sizeof(float) * np);
   add(sizeof(int4) * (size_t)total_rows);                        // selection list
   add(sizeof(int4) * (size_t)total_rows);                        // rescan list
+  const int n_items = bh->tile_off[np] / kCtaWarps;
+  add(sizeof(int) * (size_t)std::max(n_items, 1));               // work-item order
+  add(sizeof(int) * (size_t)std::max(n_items, 1));               // work-item cost
   if ((rc = ensure_workspace(h, bytes))) return rc;
   Arena ar;
   ar.base = h->ws->dev;
@@ -640,6 +643,15 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   bh->src_max_norm = ar.take<float>(np);
   int4 *sel_list_d = ar.take<int4>(total_rows);
   int4 *scan_list_d = ar.take<int4>(total_rows);
+  int *item_order_d = ar.take<int>((size_t)std::max(n_items, 1));
+  int *item_cost_d = ar.take<int>((size_t)std::max(n_items, 1));
+  {
+    std::vector<int> ord(std::max(n_items, 1));
+    for (int i = 0; i < (int)ord.size(); i++) ord[i] = i;
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(item_order_d, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice,
+                                    h->stream));
+    CVO_CUDA_TRY(h, cudaMemsetAsync(item_cost_d, 0, sizeof(int) * ord.size(), h->stream));
+  }
   // zero counters of every pair
   for (int p = 0; p < np; p++) CVO_CUDA_TRY(h, cudaMemsetAsync(bh->pairs[p].counter, 0, 2 * sizeof(unsigned), h->stream));
   for (auto &u : uploads) CVO_CUDA_TRY(h, cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, h->stream));
@@ -678,6 +690,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   B.sel_count = ctr_d + 4;
   B.scan_count = ctr_d + 5;
   B.assoc_next = ctr_d + 6;
+  B.n_items = n_items;
+  B.item_order = item_order_d;
+  B.item_cost = item_cost_d;
   {
     int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
     B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
@@ -703,6 +718,10 @@ void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEv
   k_transform<<<std::max(bh->xform_blocks, 1), 256, 0, h->stream>>>(B);
   mark(h, ev, 1);
   bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, bh->assoc_smem, h->stream>>>(B, K);
+  if (B.n_items > 1) {
+    k_order_items<<<1, 1024, 0, h->stream>>>(B.n_items, B.item_cost, B.item_order);
+    h->launches++;
+  }
   k_select<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
   bh->rescan<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
   k_rowsum<<<std::max((B.total_rows + 255) / 256, 1), 256, 0, h->stream>>>(B, K);

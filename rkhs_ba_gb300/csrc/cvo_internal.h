@@ -160,6 +160,11 @@ struct BatchDev {
   int4 *scan_list;                // count > ov: index-ordered rescan of the row
   int *scan_count;
   int *assoc_next;                // next association work item (persistent blocks); reset by k_transform
+  // work items (four tiles of one pair) in the order the persistent blocks take them:
+  // heaviest first by the cost each took in the previous pass (SM clock / 256)
+  int n_items;
+  int *item_order;
+  int *item_cost;
 };
 
 // ------------------------------------------------------------- host side

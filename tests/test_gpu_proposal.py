@@ -144,3 +144,27 @@ def test_trained_network_gain_over_the_grid(cvo, trained):
     assert succ(ok_learn) >= 0.75
     # the all-24 grid refines 24 hypotheses per pair; the network refines 2 (+ fallback)
     assert fb.sum() <= 2
+
+
+def test_invalid_arguments_are_rejected(cvo, small_pool):
+    from rkhs_ba_gb300._lib import CvoError
+    from rkhs_ba_gb300 import CvoPointCloud
+    net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=7)
+    T = np.tile(np.eye(4)[:3], (2, 1, 1))
+    with pytest.raises(CvoError):
+        net.train_step(small_pool, [0, 4], T, lr=0.0, seed=1)       # scene index out of range
+    with pytest.raises(CvoError):
+        net.forward_pool(small_pool, [-1], None)
+    w = net.weights()
+    with pytest.raises(ValueError):
+        net.set_weights(w[:-1])
+    s, t, _ = scenes.global_pair(n=2000, seed=9)
+    gs, gt = cvo.upload(s), cvo.upload(t)
+    empty = cvo.upload(CvoPointCloud(np.zeros((0, 3), np.float32), np.zeros((0, 5), np.float32)))
+    with pytest.raises(CvoError):
+        cvo.register_learned_batch(net, [gs], [empty], n_refine=1)  # empty target
+    with pytest.raises(CvoError):
+        cvo.register_learned_batch(net, [gs], [gt], n_refine=9)     # more refinements than hypotheses
+    # hypotheses of an empty cloud are defined (identity rotation block, centroid 0) and finite
+    H = net.hypotheses([gs], [empty])
+    assert H.shape == (1, 8, 4, 4) and np.all(np.isfinite(H))
