@@ -22,9 +22,16 @@ class CvoPointCloud:
         xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float32).reshape(-1, 3))
         n = xyz.shape[0]
         self.xyz = xyz
-        self.features = None if features is None else np.ascontiguousarray(np.asarray(features, np.float32).reshape(n, -1))
-        self.labels = None if labels is None else np.ascontiguousarray(np.asarray(labels, np.float32).reshape(n, -1))
+        self.features = None if features is None else self._rows(features, n)
+        self.labels = None if labels is None else self._rows(labels, n)
         self.geom_type = None if geom_type is None else np.ascontiguousarray(np.asarray(geom_type, np.float32).reshape(n, 2))
+
+    @staticmethod
+    def _rows(a, n):
+        """(n, k) float32; an empty cloud keeps the column count of a 2-D input."""
+        a = np.asarray(a, np.float32)
+        k = a.shape[1] if a.ndim == 2 else (a.size // n if n else 0)
+        return np.ascontiguousarray(a.reshape(n, k))
 
     # -- sizes (CvoPointCloud::num_points / feature_dimensions / num_classes)
     def num_points(self) -> int:
