@@ -118,8 +118,14 @@ class ClockSampler:
 
 
 def make_pairs(n_pairs, n_points, seed0=1000):
+    """Seeded global pairs, generated by spawned worker processes (never forked after CUDA is up)."""
     from rkhs_ba_gb300 import scenes
-    return [scenes.global_pair(n=n_points, seed=seed0 + k) for k in range(n_pairs)]
+    if n_pairs <= 1:
+        return [scenes.global_pair(n=n_points, seed=seed0 + k) for k in range(n_pairs)]
+    from concurrent.futures import ProcessPoolExecutor
+    from multiprocessing import get_context
+    with ProcessPoolExecutor(min(n_pairs, os.cpu_count() or 1), mp_context=get_context("spawn")) as ex:
+        return list(ex.map(scenes.global_pair, [n_points] * n_pairs, [seed0 + k for k in range(n_pairs)]))
 
 
 def _proposal(args, cvo):
