@@ -18,6 +18,7 @@
 // gradients and the Adam moments are FP32.  Training minimises the relaxed
 // winner-takes-all loss over the K hypotheses (0.95 on the best, 0.05 spread over
 // the others) with Adam; the whole step runs on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -81,8 +82,9 @@ __device__ inline int sample_index(uint32_t seed, int slot, int p, int n) {
 // C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]) (ReLU), with A(m, k) = A[m sam + k sak],
 // B(k, n) = B[k sbk + n sbn] and C row-major (leading dimension ldc).  A block of 4
 // warps computes a 64 x 64 tile (2 x 2 warps of 32 x 32) over the k range
-// [z kc, (z + 1) kc); with several k ranges the partial tiles are added atomically
-// into C, which the caller has zeroed.
+// [z kc, (z + 1) kc); with several k ranges (PARTIAL) each block stores its tile in
+// plane z of a [splits][M][N] workspace and k_split_sum adds the planes in z order,
+// so the result does not depend on the order in which the blocks finish.
 constexpr int kGT = 64;
 
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
@@ -105,7 +107,7 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-template <bool RELU, bool ATOMIC>
+template <bool RELU, bool PARTIAL>
 __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, int kc, const float *__restrict__ A,
                                                    long long sam, long long sak, const float *__restrict__ B,
                                                    long long sbk, long long sbn, const float *__restrict__ bias,
@@ -175,8 +177,8 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, int kc, 
         const int col = n0 + wn + 8 * n + 2 * t4 + (e & 1);
         if (row >= M || col >= N) continue;
         float v = acc[m][n][e];
-        if (ATOMIC) {
-          atomicAdd(&C[row * ldc + col], v);
+        if (PARTIAL) {
+          C[((size_t)blockIdx.z * M + row) * N + col] = v;
         } else {
           if (bias) v += bias[col];
           if (RELU) v = fmaxf(v, 0.f);
@@ -347,9 +349,9 @@ __global__ void k_relu_bwd(long long n, const float *H, float *dH) {
   if (i < n && !(H[i] > 0.f)) dH[i] = 0.f;
 }
 
-// out[c] += sum_r D[r][c] (out zeroed by the caller): 8 row groups per block of
-// 32 columns and 2048 rows, one atomic per column and block
-__global__ void __launch_bounds__(256) k_colsum(int M, int N, const float *D, float *out) {
+// part[y][c] = sum of D[r][c] over the rows r of block row y (2048 rows, 8 row groups
+// of a block of 32 columns added in a fixed order)
+__global__ void __launch_bounds__(256) k_colsum(int M, int N, const float *D, float *part) {
   const int c = blockIdx.x * 32 + (threadIdx.x & 31), g = threadIdx.x >> 5;
   const int r0 = blockIdx.y * 2048, r1 = min(M, r0 + 2048);
   __shared__ float red[8][33];
@@ -361,7 +363,26 @@ __global__ void __launch_bounds__(256) k_colsum(int M, int N, const float *D, fl
   if (g == 0 && c < N) {
     float t = 0.f;
     for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
-    atomicAdd(&out[c], t);
+    part[(size_t)blockIdx.y * N + c] = t;
+  }
+}
+
+// C[i / N][i % N] = sum over z of part[z][i], i < M N: warp g of a block of 32 outputs
+// adds the planes z = g, g + 8, ... and the 8 warp sums are added in warp order.
+__global__ void __launch_bounds__(256) k_split_sum(int M, int N, int splits, const float *part, float *C,
+                                                   long long ldc) {
+  const long long mn = (long long)M * N, i = blockIdx.x * 32LL + (threadIdx.x & 31);
+  const int g = threadIdx.x >> 5;
+  __shared__ float red[8][33];
+  float s = 0.f;
+  if (i < mn)
+    for (int z = g; z < splits; z += 8) s += part[z * mn + i];
+  red[g][threadIdx.x & 31] = s;
+  __syncthreads();
+  if (g == 0 && i < mn) {
+    float t = 0.f;
+    for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
+    C[(i / N) * ldc + i % N] = t;
   }
 }
 
@@ -390,6 +411,8 @@ struct NetDev {
   float *X = nullptr, *H1 = nullptr, *H2 = nullptr, *G = nullptr, *H3 = nullptr, *O = nullptr;
   float *dO = nullptr, *dH3 = nullptr, *dG = nullptr, *dH2 = nullptr, *dH1 = nullptr, *loss = nullptr;
   float *Tout = nullptr;
+  float *part = nullptr;                 // split-K and column-sum partials of the backward pass
+  size_t part_cap = 0;
   int *arg = nullptr, *best = nullptr;
 };
 
@@ -402,6 +425,9 @@ static void net_free_acts(NetDev *n) {
   cudaFree(n->slots);
   cudaFree(n->arg);
   cudaFree(n->best);
+  cudaFree(n->part);
+  n->part = nullptr;
+  n->part_cap = 0;
   n->mean = n->cent = n->X = n->H1 = n->H2 = n->G = n->H3 = n->O = nullptr;
   n->dO = n->dH3 = n->dG = n->dH2 = n->dH1 = n->loss = n->Tout = nullptr;
   n->slots = nullptr;
@@ -445,27 +471,43 @@ static int net_ensure(Handle *h, NetDev *n, int Bn) {
   return 0;
 }
 
-// C = A B (+bias, ReLU) on the tensor cores; with splits > 1 C must be zero and the
-// k range is split over blockIdx.z with atomic accumulation.
+// Number of k ranges gemm() uses for a requested split count (ranges of whole
+// 16-wide k steps).
+static int gemm_splits(long long K, int splits) {
+  const long long kc = ((K + splits - 1) / splits + 15) / 16 * 16;
+  return (int)((K + kc - 1) / kc);
+}
+
+// C = A B (+bias, ReLU) on the tensor cores; with splits > 1 the k range is split over
+// blockIdx.z, the partial tiles go to part (gemm_splits(K, splits) M N floats) and are
+// added in a fixed order.
 static void gemm(Handle *h, bool relu, int M, int N, int K, const float *A, long long sam, long long sak,
                  const float *B, long long sbk, long long sbn, const float *bias, float *C, long long ldc,
-                 int splits = 1) {
+                 int splits = 1, float *part = nullptr) {
   const int kc = ((K + splits - 1) / splits + 15) / 16 * 16;
   splits = (K + kc - 1) / kc;
   const dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, splits);
-  if (splits > 1)
-    k_gemm_bf16<false, true><<<grid, 128, 0, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, nullptr, C, ldc);
-  else if (relu)
+  if (splits > 1) {
+    k_gemm_bf16<false, true><<<grid, 128, 0, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, nullptr, part, N);
+    k_split_sum<<<(unsigned)(((long long)M * N + 31) / 32), 256, 0, h->stream>>>(M, N, splits, part, C, ldc);
+    h->launches++;
+  } else if (relu) {
     k_gemm_bf16<true, false><<<grid, 128, 0, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, bias, C, ldc);
-  else
+  } else {
     k_gemm_bf16<false, false><<<grid, 128, 0, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, bias, C, ldc);
+  }
   h->launches++;
 }
 
-static void colsum(Handle *h, int M, int N, const float *D, float *out) {
-  const dim3 grid((N + 31) / 32, (M + 2047) / 2048);
-  k_colsum<<<grid, 256, 0, h->stream>>>(M, N, D, out);
-  h->launches++;
+// Row blocks of colsum(): its workspace holds colsum_blocks(M) N floats.
+static int colsum_blocks(long long M) { return (int)std::max<long long>(1, (M + 2047) / 2048); }
+
+// out[c] = sum_r D[r][c], in a fixed order.
+static void colsum(Handle *h, int M, int N, const float *D, float *out, float *part) {
+  const int ry = colsum_blocks(M);
+  k_colsum<<<dim3((N + 31) / 32, ry), 256, 0, h->stream>>>(M, N, D, part);
+  k_split_sum<<<(N + 31) / 32, 256, 0, h->stream>>>(1, N, ry, part, out, N);
+  h->launches += 2;
 }
 
 int net_create(Handle *h, int P, unsigned seed, NetDev **out) {
@@ -633,35 +675,51 @@ int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *s
   const long long rows = (long long)S * P;
   const float *w = n->w;
   float *g = n->g;
-  CVO_CUDA_TRY(h, cudaMemsetAsync(g, 0, sizeof(float) * kNetParams, h->stream));
-  k_wta_loss<<<(Bn + 127) / 128, 128, 0, h->stream>>>(Bn, n->O, n->slots, n->cent, n->dO, n->loss, n->best);
-  h->launches++;
-  // head: O = H3 W4 + b4, H3 = relu(G' W3 + b3) with G' = G as Bn x 256
-  gemm(h, false, kNetH3, kNetOut, Bn, n->H3, 1, kNetH3, n->dO, kNetOut, 1, nullptr, g + kOffW4, kNetOut, 2);
-  colsum(h, Bn, kNetOut, n->dO, g + kOffB4);
-  gemm(h, false, Bn, kNetH3, kNetOut, n->dO, kNetOut, 1, w + kOffW4, 1, kNetOut, nullptr, n->dH3, kNetH3);
-  k_relu_bwd<<<(unsigned)(((long long)Bn * kNetH3 + 255) / 256), 256, 0, h->stream>>>((long long)Bn * kNetH3, n->H3,
-                                                                                      n->dH3);
-  gemm(h, false, kNetHead, kNetH3, Bn, n->G, 1, kNetHead, n->dH3, kNetH3, 1, nullptr, g + kOffW3, kNetH3, 2);
-  colsum(h, Bn, kNetH3, n->dH3, g + kOffB3);
-  gemm(h, false, Bn, kNetHead, kNetH3, n->dH3, kNetH3, 1, w + kOffW3, 1, kNetH3, nullptr, n->dG, kNetHead);
-  // encoder: the max-pool routes dG to the pooled rows, then two ReLU layers
-  CVO_CUDA_TRY(h, cudaMemsetAsync(n->dH2, 0, sizeof(float) * rows * kNetH2, h->stream));
-  k_maxpool_bwd<<<(S * kNetH2 + 255) / 256, 256, 0, h->stream>>>(S, P, n->G, n->dG, n->arg, n->dH2);
-  // split the row range of the weight gradients so that about 4 blocks per SM run,
-  // each over at least 64 rows
+  // split the row range of the encoder's weight gradients so that about 4 blocks per
+  // SM run, each over at least 64 rows
   const int sms = h->num_sms > 0 ? h->num_sms : 152;
   auto split_for = [&](int tiles) {
     return (int)std::max<long long>(1, std::min<long long>((4LL * sms + tiles - 1) / tiles, rows / 64));
   };
-  gemm(h, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2,
-       split_for(2));
-  colsum(h, (int)rows, kNetH2, n->dH2, g + kOffB2);
+  const int sp2 = split_for(2), sp1 = split_for(1);
+  const size_t need = std::max<size_t>(
+      {(size_t)gemm_splits(Bn, 2) * std::max(kNetH3 * kNetOut, kNetHead * kNetH3), (size_t)gemm_splits(rows, sp2) * kNetH1 * kNetH2,
+       (size_t)gemm_splits(rows, sp1) * kNetIn * kNetH1, (size_t)colsum_blocks(rows) * kNetH2,
+       (size_t)colsum_blocks(Bn) * std::max(kNetOut, kNetH3)});
+  if (need > n->part_cap) {
+    cudaFree(n->part);
+    n->part = nullptr;
+    n->part_cap = 0;
+    if (cudaMalloc((void **)&n->part, sizeof(float) * need) != cudaSuccess) {
+      cudaGetLastError();
+      h->last_error = "out of device memory for the proposal network's gradient partials";
+      return CVO_ERR_OUT_OF_MEMORY;
+    }
+    n->part_cap = need;
+  }
+  float *part = n->part;
+  k_wta_loss<<<(Bn + 127) / 128, 128, 0, h->stream>>>(Bn, n->O, n->slots, n->cent, n->dO, n->loss, n->best);
+  h->launches++;
+  // head: O = H3 W4 + b4, H3 = relu(G' W3 + b3) with G' = G as Bn x 256
+  gemm(h, false, kNetH3, kNetOut, Bn, n->H3, 1, kNetH3, n->dO, kNetOut, 1, nullptr, g + kOffW4, kNetOut, 2, part);
+  colsum(h, Bn, kNetOut, n->dO, g + kOffB4, part);
+  gemm(h, false, Bn, kNetH3, kNetOut, n->dO, kNetOut, 1, w + kOffW4, 1, kNetOut, nullptr, n->dH3, kNetH3);
+  k_relu_bwd<<<(unsigned)(((long long)Bn * kNetH3 + 255) / 256), 256, 0, h->stream>>>((long long)Bn * kNetH3, n->H3,
+                                                                                      n->dH3);
+  gemm(h, false, kNetHead, kNetH3, Bn, n->G, 1, kNetHead, n->dH3, kNetH3, 1, nullptr, g + kOffW3, kNetH3, 2, part);
+  colsum(h, Bn, kNetH3, n->dH3, g + kOffB3, part);
+  gemm(h, false, Bn, kNetHead, kNetH3, n->dH3, kNetH3, 1, w + kOffW3, 1, kNetH3, nullptr, n->dG, kNetHead);
+  // encoder: the max-pool routes dG to the pooled rows, then two ReLU layers
+  CVO_CUDA_TRY(h, cudaMemsetAsync(n->dH2, 0, sizeof(float) * rows * kNetH2, h->stream));
+  k_maxpool_bwd<<<(S * kNetH2 + 255) / 256, 256, 0, h->stream>>>(S, P, n->G, n->dG, n->arg, n->dH2);
+  gemm(h, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2, sp2,
+       part);
+  colsum(h, (int)rows, kNetH2, n->dH2, g + kOffB2, part);
   gemm(h, false, (int)rows, kNetH1, kNetH2, n->dH2, kNetH2, 1, w + kOffW2, 1, kNetH2, nullptr, n->dH1, kNetH1);
   k_relu_bwd<<<(unsigned)((rows * kNetH1 + 255) / 256), 256, 0, h->stream>>>(rows * kNetH1, n->H1, n->dH1);
-  gemm(h, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1,
-       split_for(1));
-  colsum(h, (int)rows, kNetH1, n->dH1, g + kOffB1);
+  gemm(h, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1, sp1,
+       part);
+  colsum(h, (int)rows, kNetH1, n->dH1, g + kOffB1, part);
   h->launches += 3;
   if (lr > 0.f) {
     n->steps++;

@@ -100,6 +100,20 @@ def test_first_adam_step(cvo, small_pool):
     assert np.all(np.abs(w1 - w0) <= lr * 1.0001)
 
 
+def test_training_is_deterministic(cvo, small_pool):
+    """Split-K weight gradients and column sums are added in a fixed order: the same
+    seeds give bit-identical weights."""
+    ws = []
+    for _ in range(2):
+        net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=8)
+        rng = np.random.default_rng(5)
+        for step in range(3):
+            scene, T = _batch(rng, 6)
+            net.train_step(small_pool, scene, T, lr=1e-3, seed=step)
+        ws.append(net.weights())
+    assert np.array_equal(ws[0], ws[1])
+
+
 @pytest.fixture(scope="module")
 def trained(cvo):
     pool = ScenePool(*ScenePool.generate(300, 1024, seed0=2_000_000))
