@@ -6,6 +6,7 @@
   1e-3 relative, gradient blocks within 1e-2 relative L2 (FP32 accumulation order
   and the rare bfloat16 rounding it flips are the only differences);
 * the first Adam step against its closed form;
+* training is bit-reproducible for one seed (no float atomics in the backward pass);
 * training on the device from a scene pool lowers the loss and the hypotheses'
   rotation error on held-out scenes;
 * what the trained network gains: registration of held-out 50k-point-like pairs
