@@ -166,6 +166,20 @@ def scenes_pose_error(T, T_gt):
     return scenes.pose_error(T, T_gt)
 
 
+def replica_rate(units_per_rank, ms, dist=None, device="cpu"):
+    """Whole-job rate of independent replicas: the units of all ranks divided by the
+    slowest rank's milliseconds (a MAX all-reduce over the process group; dist None
+    means one process).  Returns (units/s, slowest ms)."""
+    world = 1
+    if dist is not None:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        world = dist.get_world_size()
+    return units_per_rank * world / (ms / 1000.0), ms
+
+
 def run_ours(args):
     import torch
     from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
@@ -253,13 +267,7 @@ def run_ours(args):
     launches = cvo.kernel_launches - launches0
     prof = cvo.profile_read()
     cvo.profile(False)
-    total_ms = float(np.sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    n_reg = args.pairs * args.steps * world
-    value = n_reg / (total_ms / 1000.0)
+    value, total_ms = replica_rate(args.pairs * args.steps, float(np.sum(step_ms)), dist, "cuda")
     Ts, its, fb = results[-1]
     succ = _success(Ts, pairs)
 
@@ -321,7 +329,7 @@ def run_ours(args):
         e2e_ms.append(e0.elapsed_time(e1))
         for c in hs + ht:
             c.free()
-    e2e_value = args.pairs / (float(np.mean(e2e_ms)) / 1000.0) * world
+    e2e_value, _ = replica_rate(args.pairs, float(np.mean(e2e_ms)), dist, "cuda")
 
     # ---- roofline of the association kernel
     peak, peak_kind = _peaks()
