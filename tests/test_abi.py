@@ -132,3 +132,44 @@ def test_empty_clouds_follow_reference_returns():
     assert cvo.inner_product_cpu(a, e, np.eye(4), 0.1) == 0.0
     r = cvo.align_s2t(e, a, np.eye(4))
     assert r.return_code == -1
+
+
+_NULL_OK = {                                  # defined results for NULL / zero arguments
+    "cvo_params_default": None,               # void; ignores NULL
+    "cvo_cloud_size": 0,
+    "cvo_assoc_destroy": 0, "cvo_pose_graph_destroy": 0, "cvo_proposal_destroy": 0,   # free(NULL)
+    "cvo_rotation_grid": 60,                  # count query of the icosahedral grid
+    "cvo_proposal_dims": 0,                   # p may be NULL: the fixed dimensions
+    "cvo_status_string": b"ok", "cvo_kernel_launch_count": 0, "cvo_last_error": b"", "cvo_get_stream": None,
+}
+
+_NULL_CHILD = r"""
+import ctypes as C, json, sys
+sys.path.insert(0, sys.argv[1])
+from rkhs_ba_gb300 import _lib as L
+lib = L.lib()
+out = {}
+for name, (res, args) in L.SIGNATURES.items():
+    vals = [0 if a in (C.c_int, C.c_int64, C.c_uint32, C.c_float, C.c_double) else None for a in args]
+    r = getattr(lib, name)(*vals)
+    out[name] = r.decode() if isinstance(r, bytes) else r
+print(json.dumps(out))
+"""
+
+
+def test_every_entry_point_rejects_null_arguments():
+    """All entry points called with NULL pointers and zero sizes (no GPU work is reached):
+    each returns CVO_ERR_INVALID_ARG, except the calls whose NULL behaviour is defined."""
+    import json
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _NULL_CHILD, root], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = json.loads(r.stdout.strip().splitlines()[-1])
+    assert set(got) == set(L.SIGNATURES)
+    for name, v in got.items():
+        if name in _NULL_OK:
+            want = _NULL_OK[name]
+            assert v == (want.decode() if isinstance(want, bytes) else want), (name, v)
+        else:
+            assert v == L.CVO_ERR_INVALID_ARG, (name, v)
