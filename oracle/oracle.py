@@ -32,6 +32,18 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def build_sanitized() -> str:
+    """The oracle under AddressSanitizer and UndefinedBehaviorSanitizer, in
+    oracle/_build/asan/ (same arithmetic flags)."""
+    out = os.path.join(OUT_DIR, "asan", "libcvo_oracle.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    flags = [f for f in CFLAGS if f != "-O2"] + ["-O1", "-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined",
+                                                 "-fno-sanitize-recover=undefined"]
+    cmd = ["gcc"] + flags + ["-I" + os.path.join(HERE, "..", "include"), SRC, "-o", out, "-lm"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return out
+
+
 def _lib():
     global _L
     if _L is None:

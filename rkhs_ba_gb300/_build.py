@@ -83,5 +83,49 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
+SAN_DIR = os.path.join(ROOT, "_build", "asan")
+SAN_LIB_PATH = os.path.join(SAN_DIR, "libcvo_gb300.so")
+SAN_FLAGS = ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined",
+             "-Xcompiler", "-fno-sanitize-recover=undefined", "-Xcompiler", "-fno-omit-frame-pointer"]
+
+
+def sanitizer_preload() -> str:
+    """LD_PRELOAD value with gcc's AddressSanitizer and UBSan runtimes (a sanitized
+    shared library loaded into an unsanitized Python needs them first)."""
+    libs = []
+    for name in ("libasan.so", "libubsan.so"):
+        r = subprocess.run(["gcc", "-print-file-name=" + name], capture_output=True, text=True, check=True)
+        libs.append(r.stdout.strip())
+    return " ".join(libs)
+
+
+def build_sanitized() -> str:
+    """The same library with its HOST code (parameter reader, CPU inner product, pose-graph
+    solver, argument checks) under AddressSanitizer and UndefinedBehaviorSanitizer, in
+    _build/asan/; device code is compiled as usual.  For checks of the host paths without
+    a GPU; load it with sanitizer_preload() in LD_PRELOAD."""
+    obj_dir = os.path.join(SAN_DIR, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    nvcc = _nvcc()
+    flags = ARCH + ["-O1", "-g", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off"] + SAN_FLAGS + \
+        ["-I" + os.path.join(ROOT, "include")]
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
+        r = subprocess.run([nvcc] + flags + ["-c", src, "-o", obj], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+        return obj
+
+    srcs = _sources()
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    cmd = [nvcc, "-shared", "-Xcompiler", "-fopenmp"] + SAN_FLAGS[:4] + ARCH + ["-o", SAN_LIB_PATH] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    return SAN_LIB_PATH
+
+
 if __name__ == "__main__":
     print(build(verbose=True))
