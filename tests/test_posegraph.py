@@ -93,3 +93,28 @@ def test_errors_and_gauge():
     c0, c1, it = g.optimize()
     assert c1 < 1e-16
     assert g.size() == (2, 2)
+
+
+def test_more_rejected_inputs():
+    from rkhs_ba_gb300._lib import CvoError
+    g = PoseGraphSolver()
+    bad = np.eye(4)
+    bad[0, 3] = np.nan
+    with pytest.raises(CvoError):
+        g.insert(0, bad)                              # non-finite pose
+    g.insert(0, np.eye(4))
+    with pytest.raises(CvoError):
+        g.add_between(0, 0, np.eye(4))                # a factor needs two poses
+    with pytest.raises(CvoError):
+        g.add_prior(3, np.eye(4))                     # unknown key
+    with pytest.raises(CvoError):
+        g.get(3)
+    with pytest.raises(CvoError):
+        g.add_between(0, 0, bad)
+    # re-inserting a key replaces its value; sizes count poses and factors
+    g.insert(0, _rand_pose(np.random.default_rng(5)))
+    assert g.size() == (1, 0)
+    g.add_prior(0, np.eye(4))
+    c0, c1, it = g.optimize()
+    assert c1 <= c0 and c1 < 1e-16
+    assert np.allclose(g.get(0), np.eye(4), atol=1e-9)
