@@ -173,3 +173,55 @@ def test_every_entry_point_rejects_null_arguments():
             assert v == (want.decode() if isinstance(want, bytes) else want), (name, v)
         else:
             assert v == L.CVO_ERR_INVALID_ARG, (name, v)
+
+
+_C_CLIENT = r"""
+#include <math.h>
+#include <stdio.h>
+#include "cvo_gb300.h"
+
+int main(void) {
+  cvo_params p;
+  cvo_params_default(&p);
+  cvo_handle *h = NULL;
+  if (cvo_create_with_params(&p, &h) != CVO_OK) return 1;
+  float xyz[3 * 4] = {0, 0, 0, 0.1f, 0, 0, 0, 0.1f, 0, 0, 0, 0.1f};
+  cvo_cloud c = {4, 0, 0, 3, xyz, NULL, NULL, NULL};
+  float T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  float ip = 0.f;
+  if (cvo_inner_product_cpu(h, &c, &c, T, 0.1f, &ip) != CVO_OK || !(ip > 0.f)) return 2;
+  cvo_pose_graph *g = NULL;
+  double I[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, Z[12] = {1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 1, 0};
+  double sig[6] = {0.1, 0.1, 0.1, 0.1, 0.1, 0.1}, c0, c1, X[12];
+  int it;
+  if (cvo_pose_graph_create(&g) || cvo_pose_graph_insert(g, 0, I) || cvo_pose_graph_insert(g, 1, I) ||
+      cvo_pose_graph_add_prior(g, 0, I, sig) || cvo_pose_graph_add_between(g, 0, 1, Z, sig) ||
+      cvo_pose_graph_optimize(g, 50, &c0, &c1, &it) || cvo_pose_graph_get(g, 1, X)) return 3;
+  if (fabs(X[3] - 1.0) > 1e-9 || c1 > 1e-16) return 4;
+  cvo_pose_graph_destroy(g);
+  if (cvo_inner_product_cpu(NULL, &c, &c, T, 0.1f, &ip) != CVO_ERR_INVALID_ARG) return 5;
+  printf("%s %.6g\n", cvo_status_string(CVO_OK), (double)ip);
+  cvo_destroy(h);
+  return 0;
+}
+"""
+
+
+def test_plain_c_client_links_and_runs():
+    """A C99 program built against the header (-Wall -Wextra -Werror) links the library
+    and runs its host paths; the header also compiles as C++."""
+    lib_dir = os.path.dirname(L.LIB_PATH)
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "client.c")
+        open(src, "w").write(_C_CLIENT)
+        exe = os.path.join(d, "client")
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I" + os.path.dirname(HEADER), src, "-o",
+                        exe, "-L" + lib_dir, "-lcvo_gb300", "-Wl,-rpath," + lib_dir, "-lm"], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True)
+        assert out.returncode == 0, (out.returncode, out.stderr[-2000:])
+        assert out.stdout.startswith("ok ")
+        cpp = os.path.join(d, "client.cpp")
+        open(cpp, "w").write('#include "cvo_gb300.h"\nint main() { return cvo_status_string(0) ? 0 : 1; }\n')
+        subprocess.run(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-I" + os.path.dirname(HEADER), cpp, "-o",
+                        exe + "_cpp", "-L" + lib_dir, "-lcvo_gb300", "-Wl,-rpath," + lib_dir], check=True)
+        assert subprocess.run([exe + "_cpp"]).returncode == 0
