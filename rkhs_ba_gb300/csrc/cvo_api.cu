@@ -127,7 +127,7 @@ bool parse_int(const std::string &v, int *out) {
 // "key: value" reader that sets a field only when its key is present; keys the
 // reference does not read are ignored.  Values that the reference's yaml-cpp
 // `as<T>()` would reject (e.g. "True" for an int field) give CVO_ERR_BAD_YAML.
-extern "C" int cvo_params_read_yaml(const char *path, cvo_params *p) {
+extern "C" int cvo_params_read_yaml(const char *path, cvo_params *p) try {
   if (!path || !p) return CVO_ERR_INVALID_ARG;
   std::ifstream f(path);
   if (!f.is_open()) return CVO_ERR_IO;
@@ -207,6 +207,8 @@ extern "C" int cvo_params_read_yaml(const char *path, cvo_params *p) {
       }
   }
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // --------------------------------------------------------------- handles
@@ -233,7 +235,7 @@ static int init_handle(cvo_handle *H) {
   return CVO_OK;
 }
 
-extern "C" int cvo_create_with_params(const cvo_params *p, cvo_handle **out) {
+extern "C" int cvo_create_with_params(const cvo_params *p, cvo_handle **out) try {
   if (!p || !out) return CVO_ERR_INVALID_ARG;
   *out = nullptr;
   cvo_handle *H = new cvo_handle();
@@ -242,36 +244,46 @@ extern "C" int cvo_create_with_params(const cvo_params *p, cvo_handle **out) {
   if (rc) { delete H; return rc; }
   *out = H;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_create(const char *yaml_path, cvo_handle **out) {
+extern "C" int cvo_create(const char *yaml_path, cvo_handle **out) try {
   if (!yaml_path || !out) return CVO_ERR_INVALID_ARG;
   cvo_params p;
   cvo_params_default(&p);
   int rc = cvo_params_read_yaml(yaml_path, &p);
   if (rc) return rc;
   return cvo_create_with_params(&p, out);
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_destroy(cvo_handle *H) {
+extern "C" int cvo_destroy(cvo_handle *H) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   if (H->h.stream) cudaStreamSynchronize(H->h.stream);
   free_workspace(&H->h);
   if (H->h.own_stream) cudaStreamDestroy(H->h.own_stream);
   delete H;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_get_params(const cvo_handle *H, cvo_params *out) {
+extern "C" int cvo_get_params(const cvo_handle *H, cvo_params *out) try {
   if (!H || !out) return CVO_ERR_INVALID_ARG;
   *out = H->h.params;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_write_params(cvo_handle *H, const cvo_params *p) {
+extern "C" int cvo_write_params(cvo_handle *H, const cvo_params *p) try {
   if (!H || !p) return CVO_ERR_INVALID_ARG;
   H->h.params = *p;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" const char *cvo_status_string(int s) {
@@ -294,48 +306,58 @@ extern "C" const char *cvo_status_string(int s) {
 extern "C" int64_t cvo_kernel_launch_count(const cvo_handle *H) { return H ? H->h.launches : 0; }
 extern "C" const char *cvo_last_error(const cvo_handle *H) { return H ? H->h.last_error.c_str() : ""; }
 
-extern "C" int cvo_set_stream(cvo_handle *H, void *stream) {
+extern "C" int cvo_set_stream(cvo_handle *H, void *stream) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   if (!H->h.own_stream) return CVO_ERR_CUDA;
   cudaStreamSynchronize(H->h.stream);
   H->h.stream = stream ? (cudaStream_t)stream : H->h.own_stream;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" void *cvo_get_stream(const cvo_handle *H) { return H ? (void *)H->h.stream : nullptr; }
 
-extern "C" int cvo_profile_enable(cvo_handle *H, int on) {
+extern "C" int cvo_profile_enable(cvo_handle *H, int on) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   H->h.prof.on = on != 0;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_profile_read(const cvo_handle *H, double *assoc_ms, int64_t *assoc_launches, double *assoc_bytes,
-                                int64_t *iterations) {
+                                int64_t *iterations) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   if (assoc_ms) *assoc_ms = H->h.prof.assoc_ms;
   if (assoc_launches) *assoc_launches = H->h.prof.assoc_launches;
   if (assoc_bytes) *assoc_bytes = H->h.prof.assoc_bytes;
   if (iterations) *iterations = H->h.prof.iterations;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_profile_kernels(const cvo_handle *H, double ms[5]) {
+extern "C" int cvo_profile_kernels(const cvo_handle *H, double ms[5]) try {
   if (!H || !ms) return CVO_ERR_INVALID_ARG;
   for (int k = 0; k < 5; k++) ms[k] = H->h.prof.kernel_ms[k];
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_profile_reset(cvo_handle *H) {
+extern "C" int cvo_profile_reset(cvo_handle *H) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   bool on = H->h.prof.on;
   H->h.prof = Profile();
   H->h.prof.on = on;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ----------------------------------------------------------------- clouds
-extern "C" int cvo_cloud_upload(cvo_handle *H, const cvo_cloud *c, cvo_gpu_cloud **out) {
+extern "C" int cvo_cloud_upload(cvo_handle *H, const cvo_cloud *c, cvo_gpu_cloud **out) try {
   if (!H || !c || !out) return CVO_ERR_INVALID_ARG;
   if (!H->h.stream) return CVO_ERR_CUDA;   // handle created without a CUDA device
   DevCloud *d = nullptr;
@@ -346,37 +368,45 @@ extern "C" int cvo_cloud_upload(cvo_handle *H, const cvo_cloud *c, cvo_gpu_cloud
   g->owner = H;
   *out = g;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_cloud_free(cvo_handle *H, cvo_gpu_cloud *c) {
+extern "C" int cvo_cloud_free(cvo_handle *H, cvo_gpu_cloud *c) try {
   if (!c) return CVO_ERR_INVALID_ARG;
   if (H && H->h.stream) cudaStreamSynchronize(H->h.stream);
   cloud_free(c->d);
   delete c;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_cloud_size(const cvo_gpu_cloud *c) { return c && c->d ? c->d->n : 0; }
 
-extern "C" int cvo_cloud_dims(const cvo_gpu_cloud *c, int *F, int *C, int *has_geom_type) {
+extern "C" int cvo_cloud_dims(const cvo_gpu_cloud *c, int *F, int *C, int *has_geom_type) try {
   if (!c || !c->d) return CVO_ERR_INVALID_ARG;
   if (F) *F = c->d->F;
   if (C) *C = c->d->C;
   if (has_geom_type) *has_geom_type = c->d->has_geo ? 1 : 0;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_cloud_download(cvo_handle *H, const cvo_gpu_cloud *c, float *xyz, float *features, float *labels,
-                                  float *geom_type) {
+                                  float *geom_type) try {
   if (!H || !c || !c->d) return CVO_ERR_INVALID_ARG;
   if (!H->h.stream) return CVO_ERR_CUDA;
   return cloud_download(&H->h, c->d, xyz, features, labels, geom_type);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_cloud_from_rgbd(cvo_handle *H, const uint8_t *image, int rows, int cols, int channels,
                                    const float *depth, const float intrinsic[4], float scaling_factor, const int *uv,
                                    int n_sel, const float *geom_type, int num_classes, const float *semantics,
-                                   cvo_gpu_cloud **out, int *n_points) {
+                                   cvo_gpu_cloud **out, int *n_points) try {
   if (!H || !out) return CVO_ERR_INVALID_ARG;
   if (!H->h.stream) return CVO_ERR_CUDA;
   DevCloud *d = nullptr;
@@ -389,6 +419,8 @@ extern "C" int cvo_cloud_from_rgbd(cvo_handle *H, const uint8_t *image, int rows
   *out = new cvo_gpu_cloud{d, H};
   if (n_points) *n_points = d->n;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 namespace {
@@ -435,7 +467,7 @@ void fill_assoc(cvo_assoc *a, int rows, int cols, const std::vector<int> &rowptr
 
 // ---------------------------------------------------------------- align
 extern "C" int cvo_align_batch_dev(cvo_handle *H, int n_pairs, cvo_gpu_cloud *const *srcs, cvo_gpu_cloud *const *tgts,
-                                   const float *T_init, float *T_out, int *rets, int *iters, double *secs) {
+                                   const float *T_init, float *T_out, int *rets, int *iters, double *secs) try {
   if (!H || n_pairs < 0 || (n_pairs > 0 && (!srcs || !tgts || !T_init || !T_out))) return CVO_ERR_INVALID_ARG;
   std::vector<DevCloud *> s, t;
   std::vector<float> Ti(T_init, T_init + 16 * (size_t)n_pairs);
@@ -459,6 +491,8 @@ extern "C" int cvo_align_batch_dev(cvo_handle *H, int n_pairs, cvo_gpu_cloud *co
     if (iters) iters[p] = r.iters[p];
   }
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 static int nearest_init_pose_impl(cvo_handle *H, DevCloud *s, DevCloud *t, float ell, int num_guess, int grid_kind,
@@ -501,13 +535,15 @@ static int align_dev_impl(cvo_handle *H, DevCloud *s, DevCloud *t, const float T
 }
 
 extern "C" int cvo_align_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T_init[16],
-                             float T_out[16], cvo_assoc *assoc, double *secs, int *iters) {
+                             float T_out[16], cvo_assoc *assoc, double *secs, int *iters) try {
   if (!H || !src || !tgt || !T_init || !T_out) return CVO_ERR_INVALID_ARG;
   return align_dev_impl(H, src->d, tgt->d, T_init, T_out, assoc, secs, iters, false);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_align(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
-                         float T_out[16], cvo_assoc *assoc, double *secs, int *iters) {
+                         float T_out[16], cvo_assoc *assoc, double *secs, int *iters) try {
   if (!H || !src || !tgt || !T_init || !T_out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { if (iters) *iters = 0; if (secs) *secs = 0; return CVO_OK; }
   TmpClouds tc{H, {}};
@@ -518,11 +554,13 @@ extern "C" int cvo_align(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *t
   if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
   tc.v.push_back(t);
   return align_dev_impl(H, s->d, t->d, T_init, T_out, assoc, secs, iters, false);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_align_s2t(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T_s2t[16],
                              int want_assoc, float T_out[16], cvo_assoc *assoc, double *secs, int *iters,
-                             int *ret_code) {
+                             int *ret_code) try {
   if (!H || !src || !tgt || !T_s2t || !T_out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { if (ret_code) *ret_code = -1; return CVO_OK; }
   TmpClouds tc{H, {}};
@@ -536,6 +574,8 @@ extern "C" int cvo_align_s2t(cvo_handle *H, const cvo_cloud *src, const cvo_clou
   if (rc == CVO_ZERO_GRADIENT) { if (ret_code) *ret_code = -1; return CVO_OK; }
   if (rc == CVO_OK && ret_code) *ret_code = 0;
   return rc;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ---------------------------------------------------------- inner products
@@ -552,13 +592,15 @@ static int ip_dev(cvo_handle *H, DevCloud *s, DevCloud *t, const float T[16], fl
 }
 
 extern "C" int cvo_inner_product_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16],
-                                     float ell, float *out) {
+                                     float ell, float *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   return ip_dev(H, src->d, tgt->d, T, ell, out);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_inner_product(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
-                                 float ell, float *out) {
+                                 float ell, float *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { *out = 0.f; return CVO_OK; }
   TmpClouds tc{H, {}};
@@ -569,10 +611,12 @@ extern "C" int cvo_inner_product(cvo_handle *H, const cvo_cloud *src, const cvo_
   if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
   tc.v.push_back(t);
   return ip_dev(H, s->d, t->d, T, ell, out);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_inner_product_batch_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, int n_poses,
-                                           const float *T, float ell, float *out) {
+                                           const float *T, float ell, float *out) try {
   if (!H || !src || !tgt || n_poses < 0 || (n_poses > 0 && (!T || !out))) return CVO_ERR_INVALID_ARG;
   if (n_poses == 0) return CVO_OK;
   if (src->d->n == 0 || tgt->d->n == 0) { for (int i = 0; i < n_poses; i++) out[i] = 0.f; return CVO_OK; }
@@ -584,13 +628,15 @@ extern "C" int cvo_inner_product_batch_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
   if (rc) return rc;
   for (int i = 0; i < n_poses; i++) out[i] = (float)asum[i];
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // CvoGPU::inner_product_cpu (src/cvo/CvoGPU.cpp:113-231) on the host: radius
 // search (squared radius -2 l^2 ln(sp/sigma^2), strict <), no neighbour cap, no
 // range-scaled ell; colour/semantic factors without thresholds.
 extern "C" int cvo_inner_product_cpu(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
-                                     float ell, float *out) {
+                                     float ell, float *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { *out = 0.f; return CVO_OK; }
   if (src->F != tgt->F || src->C != tgt->C) return CVO_ERR_INVALID_ARG;
@@ -675,10 +721,12 @@ extern "C" int cvo_inner_product_cpu(cvo_handle *H, const cvo_cloud *src, const 
   for (int i = 0; i < n; i++) tot += rows[i];
   *out = (float)tot;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_function_angle(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
-                                  float ell, int is_approximate, int is_gpu, float *out) {
+                                  float ell, int is_approximate, int is_gpu, float *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { *out = 0.f; return CVO_OK; }
   float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -717,19 +765,25 @@ extern "C" int cvo_function_angle(cvo_handle *H, const cvo_cloud *src, const cvo
   }
   *out = fxfz / (fx * fz);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // -------------------------------------------------------------- association
-extern "C" int cvo_assoc_create(cvo_assoc **out) {
+extern "C" int cvo_assoc_create(cvo_assoc **out) try {
   if (!out) return CVO_ERR_INVALID_ARG;
   *out = new cvo_assoc();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
-extern "C" int cvo_assoc_destroy(cvo_assoc *a) {
+extern "C" int cvo_assoc_destroy(cvo_assoc *a) try {
   delete a;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
-extern "C" int cvo_assoc_info(const cvo_assoc *a, int *rows, int *cols, int64_t *nnz, int64_t *ns, int64_t *nt) {
+extern "C" int cvo_assoc_info(const cvo_assoc *a, int *rows, int *cols, int64_t *nnz, int64_t *ns, int64_t *nt) try {
   if (!a) return CVO_ERR_INVALID_ARG;
   if (rows) *rows = a->rows;
   if (cols) *cols = a->cols;
@@ -737,8 +791,10 @@ extern "C" int cvo_assoc_info(const cvo_assoc *a, int *rows, int *cols, int64_t 
   if (ns) *ns = (int64_t)a->source_inliers.size();
   if (nt) *nt = (int64_t)a->target_inliers.size();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
-extern "C" int cvo_assoc_copy(const cvo_assoc *a, int64_t *row_ptr, int *col, float *val, int *si, int *ti) {
+extern "C" int cvo_assoc_copy(const cvo_assoc *a, int64_t *row_ptr, int *col, float *val, int *si, int *ti) try {
   if (!a) return CVO_ERR_INVALID_ARG;
   if (row_ptr && !a->row_ptr.empty()) memcpy(row_ptr, a->row_ptr.data(), sizeof(int64_t) * a->row_ptr.size());
   if (row_ptr && a->row_ptr.empty()) row_ptr[0] = 0;
@@ -747,10 +803,12 @@ extern "C" int cvo_assoc_copy(const cvo_assoc *a, int64_t *row_ptr, int *col, fl
   if (si && !a->source_inliers.empty()) memcpy(si, a->source_inliers.data(), sizeof(int) * a->source_inliers.size());
   if (ti && !a->target_inliers.empty()) memcpy(ti, a->target_inliers.data(), sizeof(int) * a->target_inliers.size());
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_compute_association(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T[16],
-                                       float ell, cvo_assoc *out) {
+                                       float ell, cvo_assoc *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) { out->rows = src->n; out->cols = tgt->n; return CVO_OK; }
   TmpClouds tc{H, {}};
@@ -770,10 +828,12 @@ extern "C" int cvo_compute_association(cvo_handle *H, const cvo_cloud *src, cons
   if (rc) return rc;
   fill_assoc(out, src->n, tgt->n, rowptr, col, val);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_compute_association_aniso_dev(cvo_handle *H, const cvo_gpu_cloud *src, const cvo_gpu_cloud *tgt,
-                                                 const float T[16], const float kernel[9], cvo_assoc *out) {
+                                                 const float T[16], const float kernel[9], cvo_assoc *out) try {
   if (!H || !src || !tgt || !T || !kernel || !out) return CVO_ERR_INVALID_ARG;
   if (!H->h.stream) return CVO_ERR_CUDA;
   std::vector<int> rowptr, col;
@@ -783,10 +843,12 @@ extern "C" int cvo_compute_association_aniso_dev(cvo_handle *H, const cvo_gpu_cl
   if (rc) return rc;
   fill_assoc(out, src->d->n, tgt->d->n, rowptr, col, val);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_compute_association_aniso(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt,
-                                             const float T[16], const float kernel[9], cvo_assoc *out) {
+                                             const float T[16], const float kernel[9], cvo_assoc *out) try {
   if (!H || !src || !tgt || !T || !kernel || !out) return CVO_ERR_INVALID_ARG;
   // compute_association_gpu returns without output for an empty cloud (CvoGPU.cu:1942-1943)
   if (src->n == 0 || tgt->n == 0) { out->rows = src->n; out->cols = tgt->n; return CVO_OK; }
@@ -798,6 +860,8 @@ extern "C" int cvo_compute_association_aniso(cvo_handle *H, const cvo_cloud *src
   if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
   tc.v.push_back(t);
   return cvo_compute_association_aniso_dev(H, s, t, T, kernel, out);
+} catch (...) {
+  return status_from_exception();
 }
 
 // ------------------------------------------------------------ rotation grids
@@ -891,7 +955,7 @@ std::vector<float> rotation_grid(int kind, int num_guess) {
 
 }  // namespace
 
-extern "C" int cvo_rotation_grid(int grid_kind, int num_guess, float *rots, int max_rots) {
+extern "C" int cvo_rotation_grid(int grid_kind, int num_guess, float *rots, int max_rots) try {
   if (grid_kind < 0 || grid_kind > 2) return CVO_ERR_INVALID_ARG;
   std::vector<float> g = rotation_grid(grid_kind, num_guess);
   int cnt = (int)(g.size() / 9);
@@ -900,6 +964,8 @@ extern "C" int cvo_rotation_grid(int grid_kind, int num_guess, float *rots, int 
     memcpy(rots, g.data(), sizeof(float) * 9 * (size_t)k);
   }
   return cnt;
+} catch (...) {
+  return status_from_exception();
 }
 
 // get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398): every grid rotation's
@@ -941,14 +1007,16 @@ static int nearest_init_pose_impl(cvo_handle *H, DevCloud *s, DevCloud *t, float
 }
 
 extern "C" int cvo_get_nearest_init_pose_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, float ell,
-                                             int num_guess, int grid_kind, float T_out[16], double *secs) {
+                                             int num_guess, int grid_kind, float T_out[16], double *secs) try {
   if (!H || !src || !tgt || !T_out || grid_kind < 0 || grid_kind > 2) return CVO_ERR_INVALID_ARG;
   if (secs) *secs = 0;
   return nearest_init_pose_impl(H, src->d, tgt->d, ell, num_guess, grid_kind, T_out, secs, nullptr);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_get_nearest_init_pose(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, float ell,
-                                         int num_guess, int grid_kind, float T_out[16], double *secs) {
+                                         int num_guess, int grid_kind, float T_out[16], double *secs) try {
   if (!H || !src || !tgt || !T_out || grid_kind < 0 || grid_kind > 2) return CVO_ERR_INVALID_ARG;
   if (secs) *secs = 0;
   if (src->n == 0 || tgt->n == 0) { for (int k = 0; k < 16; k++) T_out[k] = (k % 5 == 0) ? 1.f : 0.f; return CVO_OK; }
@@ -960,12 +1028,14 @@ extern "C" int cvo_get_nearest_init_pose(cvo_handle *H, const cvo_cloud *src, co
   if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
   tc.v.push_back(t);
   return nearest_init_pose_impl(H, s->d, t->d, ell, num_guess, grid_kind, T_out, secs, nullptr);
+} catch (...) {
+  return status_from_exception();
 }
 
 // Batched refinement of pose hypotheses, judged by the final approximate cos-angle.
 extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, int n_hyp,
                                            const float *T_init, float judge_ell, float T_out[16], int *best,
-                                           float *cos_out, double *secs) {
+                                           float *cos_out, double *secs) try {
   if (!H || !src || !tgt || n_hyp <= 0 || !T_init || !T_out) return CVO_ERR_INVALID_ARG;
   auto t0 = std::chrono::steady_clock::now();
   std::vector<DevCloud *> s(n_hyp, src->d), t(n_hyp, tgt->d);
@@ -994,12 +1064,14 @@ extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
   auto t1 = std::chrono::steady_clock::now();
   if (secs) *secs = std::chrono::duration<double>(t1 - t0).count();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ------------------------------------------------------------ autotuner
 extern "C" int cvo_autotune_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell,
                                 int reps, int max_configs, int *n_configs, float *div_r, float *div_ext, float *ms,
-                                int *best) {
+                                int *best) try {
   if (!H || !src || !tgt || !T || max_configs < 0) return CVO_ERR_INVALID_ARG;
   if (!(ell > 0.f)) ell = H->h.params.ell_init;
   std::vector<TuneConfig> cfg;
@@ -1015,18 +1087,22 @@ extern "C" int cvo_autotune_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud
   }
   if (best) *best = bi;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_tune_set(cvo_handle *H, int F, int C, int64_t rows, float div_r, float div_ext) {
+extern "C" int cvo_tune_set(cvo_handle *H, int F, int C, int64_t rows, float div_r, float div_ext) try {
   if (!H || F < 0 || C < 0 || rows < 0 || !(div_r > 0.f) || !(div_ext > 0.f)) return CVO_ERR_INVALID_ARG;
   TuneConfig c;
   c.cell_div_r = div_r;
   c.cell_div_ext = div_ext;
   H->h.tuned[tune_key(F, C, rows)] = c;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_tune_get(const cvo_handle *H, int F, int C, int64_t rows, float *div_r, float *div_ext) {
+extern "C" int cvo_tune_get(const cvo_handle *H, int F, int C, int64_t rows, float *div_r, float *div_ext) try {
   if (!H || !div_r || !div_ext) return CVO_ERR_INVALID_ARG;
   TuneConfig c;
   auto it = H->h.tuned.find(tune_key(F, C, rows));
@@ -1034,11 +1110,13 @@ extern "C" int cvo_tune_get(const cvo_handle *H, int F, int C, int64_t rows, flo
   *div_r = c.cell_div_r;
   *div_ext = c.cell_div_ext;
   return it != H->h.tuned.end() ? CVO_OK : CVO_ERR_INVALID_ARG;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ----------------------------------------------------- adaptive-ell CVO
 extern "C" int cvo_align_adaptive_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T_init[16],
-                                      float T_out[16], double *secs, int *iters, double *trace, int trace_len) {
+                                      float T_out[16], double *secs, int *iters, double *trace, int trace_len) try {
   if (!H || !src || !tgt || !T_init || !T_out || trace_len < 0 || (trace_len > 0 && !trace)) return CVO_ERR_INVALID_ARG;
   if (src->d->n == 0 || tgt->d->n == 0) {
     if (iters) *iters = 0;
@@ -1046,10 +1124,12 @@ extern "C" int cvo_align_adaptive_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu
     return CVO_ERR_EMPTY_CLOUD;
   }
   return run_align_adaptive(&H->h, src->d, tgt->d, T_init, T_out, secs, iters, trace, trace_len);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_align_adaptive(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt, const float T_init[16],
-                                  float T_out[16], double *secs, int *iters) {
+                                  float T_out[16], double *secs, int *iters) try {
   if (!H || !src || !tgt || !T_init || !T_out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) {
     if (iters) *iters = 0;
@@ -1064,10 +1144,12 @@ extern "C" int cvo_align_adaptive(cvo_handle *H, const cvo_cloud *src, const cvo
   if ((rc = cvo_cloud_upload(H, tgt, &t))) return rc;
   tc.v.push_back(t);
   return run_align_adaptive(&H->h, s->d, t->d, T_init, T_out, secs, iters, nullptr, 0);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_compute_association_adaptive(cvo_handle *H, const cvo_cloud *src, const cvo_cloud *tgt,
-                                                const float T[16], float ell, cvo_assoc *out) {
+                                                const float T[16], float ell, cvo_assoc *out) try {
   if (!H || !src || !tgt || !T || !out) return CVO_ERR_INVALID_ARG;
   if (src->n == 0 || tgt->n == 0) {
     fill_assoc(out, src->n, tgt->n, std::vector<int>((size_t)src->n + 1, 0), {}, {});
@@ -1085,58 +1167,74 @@ extern "C" int cvo_compute_association_adaptive(cvo_handle *H, const cvo_cloud *
   if ((rc = run_association_adaptive(&H->h, s->d, t->d, T, ell, &rp, &col, &val))) return rc;
   fill_assoc(out, src->n, tgt->n, rp, col, val);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ------------------------------------------------------ learned proposal
 struct cvo_proposal { NetDev *n; };
 
-extern "C" int cvo_proposal_create(cvo_handle *H, int points_per_cloud, uint32_t seed, cvo_proposal **out) {
+extern "C" int cvo_proposal_create(cvo_handle *H, int points_per_cloud, uint32_t seed, cvo_proposal **out) try {
   if (!H || !out || points_per_cloud < 1 || points_per_cloud > 65536) return CVO_ERR_INVALID_ARG;
   NetDev *n = nullptr;
   int rc = net_create(&H->h, points_per_cloud, seed, &n);
   if (rc) return rc;
   *out = new cvo_proposal{n};
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_proposal_destroy(cvo_proposal *p) {
+extern "C" int cvo_proposal_destroy(cvo_proposal *p) try {
   if (!p) return CVO_OK;
   net_destroy(p->n);
   delete p;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_proposal_dims(const cvo_proposal *p, int *num_params, int *points_per_cloud, int *num_hyp) {
+extern "C" int cvo_proposal_dims(const cvo_proposal *p, int *num_params, int *points_per_cloud, int *num_hyp) try {
   if (num_params) *num_params = (int)net_num_params();
   if (points_per_cloud) *points_per_cloud = p ? net_points(p->n) : 0;
   if (num_hyp) *num_hyp = 8;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_proposal_get(cvo_handle *H, cvo_proposal *p, int which, float *out) {
+extern "C" int cvo_proposal_get(cvo_handle *H, cvo_proposal *p, int which, float *out) try {
   if (!H || !p || !out) return CVO_ERR_INVALID_ARG;
   return net_get(&H->h, p->n, which, out);
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_proposal_set(cvo_handle *H, cvo_proposal *p, const float *weights) {
+extern "C" int cvo_proposal_set(cvo_handle *H, cvo_proposal *p, const float *weights) try {
   if (!H || !p || !weights) return CVO_ERR_INVALID_ARG;
   return net_set(&H->h, p->n, weights);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_proposal_train_pool_dev(cvo_handle *H, cvo_proposal *p, int n_scenes, int n_pts,
                                            const float *src_pts, const float *tgt_pts, int n_pairs, const int *scene,
-                                           const float *T_label, float lr, uint32_t seed, float *loss) {
+                                           const float *T_label, float lr, uint32_t seed, float *loss) try {
   if (!H || !p) return CVO_ERR_INVALID_ARG;
   return net_train_pool(&H->h, p->n, n_scenes, n_pts, src_pts, tgt_pts, n_pairs, scene, T_label, lr, seed, loss);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_proposal_forward_pool_dev(cvo_handle *H, cvo_proposal *p, int n_scenes, int n_pts,
                                              const float *src_pts, const float *tgt_pts, int n_pairs,
                                              const int *scene, const float *T_tgt, uint32_t seed, float *raw_out,
-                                             float *T_out) {
+                                             float *T_out) try {
   if (!H || !p) return CVO_ERR_INVALID_ARG;
   return net_forward_pool(&H->h, p->n, n_scenes, n_pts, src_pts, tgt_pts, n_pairs, scene, T_tgt, seed, raw_out,
                           T_out);
+} catch (...) {
+  return status_from_exception();
 }
 
 static int collect_clouds(int n, cvo_gpu_cloud *const *a, std::vector<DevCloud *> *out) {
@@ -1149,12 +1247,14 @@ static int collect_clouds(int n, cvo_gpu_cloud *const *a, std::vector<DevCloud *
 }
 
 extern "C" int cvo_proposal_hypotheses_dev(cvo_handle *H, cvo_proposal *p, int n_pairs, cvo_gpu_cloud *const *srcs,
-                                           cvo_gpu_cloud *const *tgts, uint32_t seed, float *T_out) {
+                                           cvo_gpu_cloud *const *tgts, uint32_t seed, float *T_out) try {
   if (!H || !p || n_pairs <= 0 || !srcs || !tgts || !T_out) return CVO_ERR_INVALID_ARG;
   std::vector<DevCloud *> s, t;
   int rc;
   if ((rc = collect_clouds(n_pairs, srcs, &s)) || (rc = collect_clouds(n_pairs, tgts, &t))) return rc;
   return net_hypotheses(&H->h, p->n, n_pairs, s.data(), t.data(), seed, T_out);
+} catch (...) {
+  return status_from_exception();
 }
 
 // Global registration of n_pairs pairs from the network's hypotheses: every pair's
@@ -1168,7 +1268,7 @@ extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, in
                                               cvo_gpu_cloud *const *srcs, cvo_gpu_cloud *const *tgts, int n_refine,
                                               float rank_ell, float judge_ell, float fallback_cos, float refine_ell,
                                               uint32_t seed, float *T_out, float *cos_out, int *used_fallback,
-                                              int *iters, double *secs) {
+                                              int *iters, double *secs) try {
   constexpr int kHyp = 8;
   if (!H || !p || n_pairs <= 0 || !srcs || !tgts || !T_out || n_refine < 1 || n_refine > kHyp)
     return CVO_ERR_INVALID_ARG;
@@ -1287,12 +1387,14 @@ extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, in
   }
   if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 // ------------------------------------------------------------ multi-frame
 extern "C" int cvo_align_multi_dev(cvo_handle *H, int n_frames, cvo_gpu_cloud *const *clouds, double *poses,
                                    const uint8_t *hold_const, int n_edges, const int *edges, double *secs,
-                                   int *iters) {
+                                   int *iters) try {
   if (!H || n_frames <= 0 || !clouds || !poses || !hold_const || n_edges < 0 || (n_edges > 0 && !edges))
     return CVO_ERR_INVALID_ARG;
   std::vector<DevCloud *> c(n_frames);
@@ -1304,10 +1406,12 @@ extern "C" int cvo_align_multi_dev(cvo_handle *H, int n_frames, cvo_gpu_cloud *c
     if (edges[2 * e] < 0 || edges[2 * e] >= n_frames || edges[2 * e + 1] < 0 || edges[2 * e + 1] >= n_frames)
       return CVO_ERR_INVALID_ARG;
   return run_align_multi(&H->h, n_frames, c.data(), poses, hold_const, n_edges, edges, secs, iters);
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_align_multi(cvo_handle *H, int n_frames, const cvo_cloud *clouds, double *poses,
-                               const uint8_t *hold_const, int n_edges, const int *edges, double *secs, int *iters) {
+                               const uint8_t *hold_const, int n_edges, const int *edges, double *secs, int *iters) try {
   if (!H || n_frames <= 0 || !clouds) return CVO_ERR_INVALID_ARG;
   TmpClouds tc{H, {}};
   std::vector<cvo_gpu_cloud *> g(n_frames);
@@ -1317,4 +1421,6 @@ extern "C" int cvo_align_multi(cvo_handle *H, int n_frames, const cvo_cloud *clo
     tc.v.push_back(g[i]);
   }
   return cvo_align_multi_dev(H, n_frames, g.data(), poses, hold_const, n_edges, edges, secs, iters);
+} catch (...) {
+  return status_from_exception();
 }

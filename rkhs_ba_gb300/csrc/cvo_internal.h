@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <map>
+#include <new>
 #include "../../include/cvo_gb300.h"
 
 namespace cvo_gb {
@@ -312,5 +313,17 @@ int set_cuda_error(Handle *h, cudaError_t e, const char *where);
     cudaError_t e__ = (call);                                      \
     if (e__ != cudaSuccess) return set_cuda_error((h), e__, #call); \
   } while (0)
+
+// Status of the exception being handled: the C entry points catch everything, so no
+// C++ exception crosses the C ABI (host allocation failure -> out of memory).
+inline int status_from_exception() {
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    return CVO_ERR_OUT_OF_MEMORY;
+  } catch (...) {
+    return CVO_ERR_INVALID_ARG;
+  }
+}
 
 }  // namespace cvo_gb

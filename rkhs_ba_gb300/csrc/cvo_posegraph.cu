@@ -336,18 +336,22 @@ static bool finite12(const double *p) {
   return true;
 }
 
-extern "C" int cvo_pose_graph_create(cvo_pose_graph **out) {
+extern "C" int cvo_pose_graph_create(cvo_pose_graph **out) try {
   if (!out) return CVO_ERR_INVALID_ARG;
   *out = new cvo_pose_graph();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_destroy(cvo_pose_graph *g) {
+extern "C" int cvo_pose_graph_destroy(cvo_pose_graph *g) try {
   delete g;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_insert(cvo_pose_graph *g, int64_t key, const double pose[12]) {
+extern "C" int cvo_pose_graph_insert(cvo_pose_graph *g, int64_t key, const double pose[12]) try {
   if (!g || !finite12(pose)) return CVO_ERR_INVALID_ARG;
   PoseGraphSolver &s = g->s;
   auto it = s.index.find(key);
@@ -359,9 +363,11 @@ extern "C" int cvo_pose_graph_insert(cvo_pose_graph *g, int64_t key, const doubl
     s.X.push_back(pose_from12(pose));
   }
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_add_prior(cvo_pose_graph *g, int64_t key, const double pose[12], const double sigmas[6]) {
+extern "C" int cvo_pose_graph_add_prior(cvo_pose_graph *g, int64_t key, const double pose[12], const double sigmas[6]) try {
   if (!g || !finite12(pose) || !valid_sigmas(sigmas)) return CVO_ERR_INVALID_ARG;
   if (g->s.index.find(key) == g->s.index.end()) return CVO_ERR_INVALID_ARG;
   Factor f;
@@ -372,10 +378,12 @@ extern "C" int cvo_pose_graph_add_prior(cvo_pose_graph *g, int64_t key, const do
   g->s.factors.push_back(f);
   g->s.has_prior = true;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_pose_graph_add_between(cvo_pose_graph *g, int64_t from, int64_t to, const double rel[12],
-                                          const double sigmas[6]) {
+                                          const double sigmas[6]) try {
   if (!g || !finite12(rel) || !valid_sigmas(sigmas) || from == to) return CVO_ERR_INVALID_ARG;
   if (g->s.index.find(from) == g->s.index.end() || g->s.index.find(to) == g->s.index.end()) return CVO_ERR_INVALID_ARG;
   Factor f;
@@ -386,31 +394,41 @@ extern "C" int cvo_pose_graph_add_between(cvo_pose_graph *g, int64_t from, int64
   for (int k = 0; k < 6; k++) f.isig[k] = 1.0 / sigmas[k];
   g->s.factors.push_back(f);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
 extern "C" int cvo_pose_graph_optimize(cvo_pose_graph *g, int max_iters, double *initial_cost, double *final_cost,
-                                       int *iters) {
+                                       int *iters) try {
   if (!g || max_iters < 0) return CVO_ERR_INVALID_ARG;
   return g->s.optimize(max_iters, initial_cost, final_cost, iters);
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_get(const cvo_pose_graph *g, int64_t key, double pose[12]) {
+extern "C" int cvo_pose_graph_get(const cvo_pose_graph *g, int64_t key, double pose[12]) try {
   if (!g || !pose) return CVO_ERR_INVALID_ARG;
   auto it = g->s.index.find(key);
   if (it == g->s.index.end()) return CVO_ERR_INVALID_ARG;
   pose_to12(g->s.X[it->second], pose);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_size(const cvo_pose_graph *g, int *n_poses, int *n_factors) {
+extern "C" int cvo_pose_graph_size(const cvo_pose_graph *g, int *n_poses, int *n_factors) try {
   if (!g) return CVO_ERR_INVALID_ARG;
   if (n_poses) *n_poses = (int)g->s.X.size();
   if (n_factors) *n_factors = (int)g->s.factors.size();
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
 
-extern "C" int cvo_pose_graph_cost(const cvo_pose_graph *g, double *cost) {
+extern "C" int cvo_pose_graph_cost(const cvo_pose_graph *g, double *cost) try {
   if (!g || !cost) return CVO_ERR_INVALID_ARG;
   *cost = g->s.cost(g->s.X);
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
 }
