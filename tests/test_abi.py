@@ -225,3 +225,25 @@ def test_plain_c_client_links_and_runs():
         subprocess.run(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-I" + os.path.dirname(HEADER), cpp, "-o",
                         exe + "_cpp", "-L" + lib_dir, "-lcvo_gb300", "-Wl,-rpath," + lib_dir], check=True)
         assert subprocess.run([exe + "_cpp"]).returncode == 0
+
+
+_OOM_CHILD = r"""
+import resource, sys
+sys.path.insert(0, sys.argv[1])
+from rkhs_ba_gb300 import _lib as L
+lib = L.lib()
+assert lib.cvo_rotation_grid(2, 3, None, 0) == 27
+vm_kb = [int(l.split()[1]) for l in open("/proc/self/status") if l.startswith("VmSize:")][0]
+soft, hard = resource.getrlimit(resource.RLIMIT_AS)
+resource.setrlimit(resource.RLIMIT_AS, (vm_kb * 1024 + (256 << 20), hard))
+print(lib.cvo_rotation_grid(2, 300, None, 0))      # 27 M rotations, about 1 GB: cannot fit
+"""
+
+
+def test_host_allocation_failure_returns_a_status():
+    """A host allocation that fails inside an entry point (address space capped in a
+    child process) returns CVO_ERR_OUT_OF_MEMORY instead of ending the process."""
+    import sys
+    r = subprocess.run([sys.executable, "-c", _OOM_CHILD, ROOT], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert int(r.stdout.strip().splitlines()[-1]) == L.CVO_ERR_OUT_OF_MEMORY
