@@ -52,6 +52,24 @@ def _profile_value(name, key):
     return None
 
 
+def issue_roofline(inst_per_pair, pair_passes, launches, avg_launch_s, sms, sm_mhz):
+    """Instruction-issue bound of the association phase: k_assoc_cta's warp instructions
+    per launch (the ncu capture's count per pair-launch times this run's mean pairs per
+    launch) over the event-timed phase duration, against one warp instruction per
+    cycle on each of an SM's 4 schedulers at the sampled SM clock.  None when an input
+    is missing."""
+    if not inst_per_pair or pair_passes <= 0 or launches <= 0 or not avg_launch_s or avg_launch_s <= 0 \
+            or not sms or not sm_mhz:
+        return None
+    inst = inst_per_pair * pair_passes / launches
+    achieved = inst / avg_launch_s / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"achieved": round(achieved, 2), "peak": round(peak, 2), "unit": "G warp instructions/s",
+            "frac": round(achieved / peak, 4), "warp_instructions_per_launch": round(inst),
+            "note": "k_assoc_cta instructions from profiles/k_assoc_cta_global50k.md over the whole association "
+                    "phase's duration; peak = SMs x 4 schedulers x SM clock"}
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -351,6 +369,13 @@ def run_ours(args):
                 "kernel": "k_assoc_cta + k_select + k_rescan + k_rowsum", "launches": prof["assoc_launches"],
                 "avg_launch_us": round(avg_s * 1e6, 3), "algorithmic_bytes_per_launch": round(per_launch_bytes),
                 "iteration_kernel_ms": {k: round(v, 3) for k, v in prof["kernel_ms"].items()}}
+        try:
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+        except Exception:
+            sms = None
+        roof["issue"] = issue_roofline(_profile_value("k_assoc_cta_global50k.md", "warp_instructions_per_pair_launch"),
+                                       pair_passes, prof["assoc_launches"], avg_s, sms,
+                                       clk.get("sm_mhz") or clk.get("sm_max_mhz"))
 
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,

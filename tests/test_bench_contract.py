@@ -40,3 +40,19 @@ def test_reference_arm_prints_one_contract_line():
 
 def test_reference_arm_other_ranks_are_silent():
     assert _run({"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_issue_roofline_arithmetic():
+    sys.path.insert(0, ROOT)
+    import bench
+    # 2 pair-passes over 1 launch of 1 ms, 1e6 warp instructions per pair; 152 SMs at 2000 MHz
+    r = bench.issue_roofline(1e6, 2, 1, 1e-3, 152, 2000.0)
+    assert r["warp_instructions_per_launch"] == 2000000
+    assert r["achieved"] == 2.0                        # 2e6 / 1e-3 s = 2 G warp instructions / s
+    assert r["peak"] == 1216.0                         # 152 x 4 x 2.0 GHz
+    assert abs(r["frac"] - 2.0 / 1216.0) < 1e-4
+    assert bench.issue_roofline(None, 2, 1, 1e-3, 152, 2000.0) is None
+    assert bench.issue_roofline(1e6, 0, 1, 1e-3, 152, 2000.0) is None
+    assert bench.issue_roofline(1e6, 2, 1, 1e-3, None, 2000.0) is None
+    v = bench._profile_value("k_assoc_cta_global50k.md", "warp_instructions_per_pair_launch")
+    assert v is not None and v > 1e8
