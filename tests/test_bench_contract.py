@@ -1,7 +1,11 @@
-"""bench.py's reference arm on the CPU: one JSON line with the keys of the bench
-contract (metric, value, unit, n_gpus, steps, warmup, ms_per_step, higher_is_better,
-scaling, vs_baseline, dtype, data, config, e2e, cpu_baseline, impl), on a small
-bounded sample; ranks other than 0 print nothing and exit 0."""
+"""bench.py on the CPU.
+
+* The reference arm: one JSON line with the keys of the bench contract (metric, value,
+  unit, n_gpus, steps, warmup, ms_per_step, higher_is_better, scaling, vs_baseline,
+  dtype, data, config, e2e, cpu_baseline, impl) on a small bounded sample; ranks other
+  than 0 print nothing and exit 0.
+* The roofline helpers' arithmetic.
+* The GPU arm's own Python with CUDA and the GPU API faked (contract keys only)."""
 import json
 import os
 import subprocess
@@ -56,3 +60,147 @@ def test_issue_roofline_arithmetic():
     assert bench.issue_roofline(1e6, 2, 1, 1e-3, None, 2000.0) is None
     v = bench._profile_value("k_assoc_cta_global50k.md", "warp_instructions_per_pair_launch")
     assert v is not None and v > 1e8
+
+
+_FAKE_GPU_CHILD = r"""
+import json, sys
+import numpy as np
+
+
+def main():
+    sys.path.insert(0, sys.argv[1])
+    import torch
+    import bench
+    import rkhs_ba_gb300
+
+    class FakeStream:
+        cuda_stream = 0
+
+    class FakeEvent:
+        clock = 0.0
+
+        def __init__(self, enable_timing=True):
+            self.t = 0.0
+
+        def record(self, stream=None):
+            FakeEvent.clock += 25.0
+            self.t = FakeEvent.clock
+
+        def synchronize(self):
+            pass
+
+        def elapsed_time(self, other):
+            return other.t - self.t
+
+    class Props:
+        multi_processor_count = 152
+
+    torch.cuda.set_device = lambda i: None
+    torch.cuda.Stream = lambda: FakeStream()
+    torch.cuda.set_stream = lambda s: None
+    torch.cuda.Event = FakeEvent
+    torch.cuda.synchronize = lambda *a: None
+    torch.cuda.get_device_properties = lambda i: Props()
+    real_empty = torch.empty
+    torch.empty = lambda *a, device=None, **k: real_empty(*a, **k)
+
+    class FakeCloud:
+        def __init__(self, c):
+            self.c = c
+
+        def free(self):
+            pass
+
+    class FakeNet:
+        num_hyp, num_params = 8, 93704
+
+        def hypotheses(self, gs, gt):
+            return np.tile(np.eye(4, dtype=np.float32), (len(gs), 8, 1, 1))
+
+    class FakeCvo:
+        rotation_grid = staticmethod(rkhs_ba_gb300.CvoGPU.rotation_grid)
+
+        def __init__(self, params=None):
+            self.p, self.n = params, 0
+
+        def set_stream(self, s):
+            pass
+
+        def upload(self, c):
+            return FakeCloud(c)
+
+        def register_learned_batch(self, net, gs, gt, n_refine=1, fallback_cos=0.0, refine_ell=0.0):
+            self.n += 100
+            k = len(gs)
+            return np.tile(np.eye(4), (k, 1, 1)), np.ones(k), np.zeros(k, np.int32), np.full(k, 60), 0.1
+
+        def get_nearest_init_pose(self, s, t, ell, num_guess, kind):
+            return np.eye(4), 0.0
+
+        def align_batch(self, gs, gt, inits):
+            k = len(gs)
+            return np.tile(np.eye(4), (k, 1, 1)), np.zeros(k, np.int32), np.full(k, 250), 0.1
+
+        def register_hypotheses(self, s, t, Ts, ell):
+            return np.eye(4), 0, np.ones(len(Ts)), 0.1
+
+        def autotune(self, s, t, T, ell=0.0, reps=3):
+            return {"configs": [(4.0, 8.0, 2.0), (6.0, 4.0, 1.9)], "best": 1}
+
+        def profile(self, on=True):
+            pass
+
+        def profile_reset(self):
+            pass
+
+        @property
+        def kernel_launches(self):
+            return self.n
+
+        def profile_read(self):
+            return {"assoc_ms": 400.0, "assoc_launches": 80, "assoc_bytes": 4.9e8 * 80, "iterations": 60,
+                    "kernel_ms": {"transform": 1.0, "assoc": 400.0, "reduce": 5.0, "step": 50.0, "iteration": 456.0}}
+
+    class FakeClocks:
+        def __init__(self, index=0):
+            pass
+
+        def start(self):
+            pass
+
+        def stop(self):
+            return {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 10}
+
+    rkhs_ba_gb300.CvoGPU = FakeCvo
+    bench._proposal = lambda args, cvo: (FakeNet(), {"fake": True})
+    bench.ClockSampler = FakeClocks
+    sys.argv = ["bench.py", "--pairs", "2", "--points", "2000", "--steps", "3", "--warmup", "3", "--all24-pairs", "1",
+                "--cpu-rotations", "1", "--cpu-iters", "1"]
+    bench.main()
+
+
+
+if __name__ == "__main__":
+    main()
+"""
+
+
+def test_ours_arm_json_with_a_faked_gpu(tmp_path):
+    """bench.py's own Python for the GPU arm (timing loops, replica rate, e2e, roofline with
+    traffic and issue fractions, CPU baseline, JSON) run with CUDA and the library's GPU
+    API replaced by fakes: every contract key is present.  The numbers are meaningless;
+    the kernels are covered by the gpu-marked tests."""
+    script = tmp_path / "fake_gpu_bench.py"
+    script.write_text(_FAKE_GPU_CHILD)
+    r = subprocess.run([sys.executable, str(script), ROOT], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "e2e", "gpu_launches", "roofline", "cpu_baseline", "clocks"):
+        assert k in d, k
+    assert d["n_gpus"] == 1 and d["steps"] == 3 and d["warmup"] == 3
+    roof = d["roofline"]
+    assert roof["bound"] == "hbm" and roof["frac"] > 0 and roof["traffic"] > 0
+    assert roof["issue"]["frac"] > 0 and roof["issue"]["peak"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] > 0
