@@ -447,9 +447,11 @@ def cpu_baseline(args, pair, iters_per_reg, budget_s=None):
 def run_component(args):
     """Timing of one component beside the main workload (one JSON line): the multi-frame
     window solve (8 frames of 20k-60k points, all 28 edges), the association with a
-    non-isotropic kernel (50k x 50k), or the RGB-D front-end (a 1226 x 370 frame, 50k
-    selected pixels).  Each call is timed end to end (host inputs, host outputs) after
-    warm-up; the CPU oracle is timed on a bounded sample of the same input."""
+    non-isotropic kernel (50k x 50k), the RGB-D front-end (a 1226 x 370 frame, 50k
+    selected pixels), adaptive-ell CVO, the proposal network, or the held-out evaluation
+    of global registration (global-eval: learned vs plain grid over --eval-pairs pairs).
+    Each call is timed end to end after warm-up; where the oracle has the same path it is
+    timed on a bounded sample of the same input."""
     import torch
     from oracle import oracle as orc
     from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
@@ -575,6 +577,72 @@ def run_component(args):
                     "cpu_baseline": {"value": round(1.0 / cpu_sec, 6), "unit": "registrations/s", "cores": cores,
                                      "kind": "port", "sample": "%d oracle iterations scaled to the GPU's %d"
                                                                 % (q.MAX_ITER, iters)}})
+    elif args.component == "global-eval":
+        # success and registrations/s of the learned pipeline and of the plain grid (nearest
+        # of the 24 rotations by cos-angle, then align) over --eval-pairs seeded held-out
+        # pairs (seeds disjoint from the training pool and the default line's pairs),
+        # registered in batches of --pairs; clouds resident on the device
+        p = CvoParams(params_path("color"))
+        cvo = CvoGPU(params=p)
+        net, prop_info = _proposal(args, cvo)
+        n_total = max(1, args.eval_pairs)
+        pairs = make_pairs(n_total, args.points, seed0=args.eval_seed0)
+        errs = {"learned": [], "grid": []}
+        iters = {"learned": [], "grid": []}
+        secs = {"learned": 0.0, "grid": 0.0}
+        fallbacks = 0
+
+        def learned(gs, gt):
+            return cvo.register_learned_batch(net, gs, gt, n_refine=args.refine, fallback_cos=args.fallback_cos,
+                                              refine_ell=args.refine_ell)
+
+        def grid(gs, gt):
+            inits = []
+            for s, t in zip(gs, gt):
+                Tg, _ = cvo.get_nearest_init_pose(s, t, p.ell_init_first_frame, 0, 1)
+                inits.append(scenes.inv_T(Tg))
+            return cvo.align_batch(gs, gt, inits)
+
+        for b0 in range(0, n_total, args.pairs):
+            batch = pairs[b0:b0 + args.pairs]
+            gs = [cvo.upload(s) for s, _, _ in batch]
+            gt = [cvo.upload(t) for _, t, _ in batch]
+            if b0 == 0:                       # warm-up of both paths (graphs, grid levels)
+                learned(gs, gt)
+                grid(gs, gt)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Ts, _, fb, its, _ = learned(gs, gt)
+            torch.cuda.synchronize()
+            secs["learned"] += time.perf_counter() - t0
+            fallbacks += int(np.sum(fb))
+            t0 = time.perf_counter()
+            Tp, _, itp, _ = grid(gs, gt)
+            torch.cuda.synchronize()
+            secs["grid"] += time.perf_counter() - t0
+            for k, (_, _, T_gt) in enumerate(batch):
+                errs["learned"].append(scenes.pose_error(Ts[k], T_gt))
+                errs["grid"].append(scenes.pose_error(Tp[k], T_gt))
+            iters["learned"] += [int(i) for i in its]
+            iters["grid"] += [int(i) for i in itp]
+            for c in gs + gt:
+                c.free()
+        ok = {m: [bool(r < 2.0 and t < 0.05) for r, t in errs[m]] for m in errs}
+        rate = {m: n_total / secs[m] for m in secs}
+        out.update({"metric": "global registrations/s and success over held-out 50k-point pairs, learned vs plain grid",
+                    "unit": "registrations/s", "value": round(rate["learned"], 4), "pairs": n_total,
+                    "learned": {"value": round(rate["learned"], 4), "success_rate": float(np.mean(ok["learned"])),
+                                "mean_iters": float(np.mean(iters["learned"])), "fallbacks": fallbacks},
+                    "plain_grid": {"value": round(rate["grid"], 4), "success_rate": float(np.mean(ok["grid"])),
+                                   "mean_iters": float(np.mean(iters["grid"]))},
+                    "both_succeed": float(np.mean([a and b for a, b in zip(ok["learned"], ok["grid"])])),
+                    "learned_over_plain_grid": round(rate["learned"] / rate["grid"], 3),
+                    "config": {"points_per_cloud": args.points, "batch": args.pairs, "params": "color.yaml",
+                               "seeds": [args.eval_seed0, args.eval_seed0 + n_total - 1],
+                               "rotation": "uniform SO(3)", "translation_max_m": 2.0,
+                               "criterion": "rot<2deg, trans<5cm", "refine_ell": args.refine_ell,
+                               "timing": "host clock around synchronised batches, clouds resident"},
+                    "proposal": prop_info})
     elif args.component == "proposal":
         from oracle import proposal as op
         from rkhs_ba_gb300.proposal import ProposalNet, ScenePool
@@ -675,7 +743,10 @@ def main():
     ap.add_argument("--grid-steps", type=int, default=1, help="timed steps of the plain grid")
     ap.add_argument("--all24-pairs", type=int, default=2, help="pairs registered by the all-24 grid")
     ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
-    ap.add_argument("--component", default="", choices=["", "irls", "aniso", "frontend", "proposal", "adaptive"],
+    ap.add_argument("--eval-pairs", type=int, default=200, help="held-out pairs of --component global-eval")
+    ap.add_argument("--eval-seed0", type=int, default=5000, help="first seed of --component global-eval's pairs")
+    ap.add_argument("--component", default="",
+                    choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval"],
                     help="time one component instead of the main workload")
     args = ap.parse_args()
     from rkhs_ba_gb300 import _build

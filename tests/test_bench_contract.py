@@ -174,8 +174,8 @@ def main():
     rkhs_ba_gb300.CvoGPU = FakeCvo
     bench._proposal = lambda args, cvo: (FakeNet(), {"fake": True})
     bench.ClockSampler = FakeClocks
-    sys.argv = ["bench.py", "--pairs", "2", "--points", "2000", "--steps", "3", "--warmup", "3", "--all24-pairs", "1",
-                "--cpu-rotations", "1", "--cpu-iters", "1"]
+    sys.argv = ["bench.py"] + (sys.argv[2:] or ["--pairs", "2", "--points", "2000", "--steps", "3", "--warmup", "3",
+                                                "--all24-pairs", "1", "--cpu-rotations", "1", "--cpu-iters", "1"])
     bench.main()
 
 
@@ -204,3 +204,19 @@ def test_ours_arm_json_with_a_faked_gpu(tmp_path):
     assert roof["issue"]["frac"] > 0 and roof["issue"]["peak"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] > 0
+
+
+def test_global_eval_component_with_a_faked_gpu(tmp_path):
+    """bench.py --component global-eval (held-out evaluation, learned vs plain grid) runs
+    its own Python end to end with the GPU faked: batches, success rates, JSON."""
+    script = tmp_path / "fake_gpu_bench.py"
+    script.write_text(_FAKE_GPU_CHILD)
+    r = subprocess.run([sys.executable, str(script), ROOT, "--component", "global-eval", "--eval-pairs", "5",
+                        "--pairs", "2", "--points", "2000"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
+    assert d["component"] == "global-eval" and d["pairs"] == 5
+    assert d["config"]["seeds"] == [5000, 5004]
+    for m in ("learned", "plain_grid"):
+        assert d[m]["value"] > 0 and 0.0 <= d[m]["success_rate"] <= 1.0
+    assert d["learned_over_plain_grid"] > 0
