@@ -135,15 +135,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_pairs(n_pairs, n_points, seed0=1000):
-    """Seeded global pairs, generated by spawned worker processes (never forked after CUDA is up)."""
+def make_pairs(n_pairs, n_points, seed0=1000, gen=None):
+    """Seeded pairs (global pairs unless gen is another scenes generator taking (n, seed);
+    n_points may be a list of sizes), generated by spawned worker processes (never forked
+    after CUDA is up)."""
     from rkhs_ba_gb300 import scenes
+    gen = gen or scenes.global_pair
+    sizes = list(n_points) if isinstance(n_points, (list, tuple)) else [n_points] * n_pairs
     if n_pairs <= 1:
-        return [scenes.global_pair(n=n_points, seed=seed0 + k) for k in range(n_pairs)]
+        return [gen(sizes[k], seed0 + k) for k in range(n_pairs)]
     from concurrent.futures import ProcessPoolExecutor
     from multiprocessing import get_context
     with ProcessPoolExecutor(min(n_pairs, os.cpu_count() or 1), mp_context=get_context("spawn")) as ex:
-        return list(ex.map(scenes.global_pair, [n_points] * n_pairs, [seed0 + k for k in range(n_pairs)]))
+        return list(ex.map(gen, sizes[:n_pairs], [seed0 + k for k in range(n_pairs)]))
 
 
 def _proposal(args, cvo):
@@ -643,6 +647,44 @@ def run_component(args):
                                "criterion": "rot<2deg, trans<5cm", "refine_ell": args.refine_ell,
                                "timing": "host clock around synchronised batches, clouds resident"},
                     "proposal": prop_info})
+    elif args.component == "batching":
+        # one persistent batch for all registrations against one call per registration (the
+        # reference's way): (a) --pairs colour pairs of uneven size (20k-60k points), identity
+        # start; (b) the 24 grid rotations of one global pair as 24 starts of the same pair
+        p = CvoParams(params_path("color"))
+        cvo = CvoGPU(params=p)
+        sizes = [int(x) for x in np.random.default_rng(7).integers(20000, 60001, size=args.pairs)]
+        pairs = make_pairs(args.pairs, sizes, seed0=300, gen=scenes.stereo_pair)
+        gs = [cvo.upload(s) for s, _, _ in pairs]
+        gt = [cvo.upload(t) for _, t, _ in pairs]
+        gp_s, gp_t, _ = make_pairs(1, args.points, seed0=args.eval_seed0)[0]
+        hs, ht = cvo.upload(gp_s), cvo.upload(gp_t)
+        T24 = []
+        for R in CvoGPU.rotation_grid(1):
+            T = np.eye(4)
+            T[:3, :3] = R.T                   # internal pose of grid rotation R
+            T24.append(T)
+        legs = {"pairs": (gs, gt, [np.eye(4)] * len(gs)), "hypotheses": ([hs] * len(T24), [ht] * len(T24), T24)}
+        res, out_legs = {}, {}
+        for name, (S, Tt, inits) in legs.items():
+            def batched():
+                res["b"] = cvo.align_batch(S, Tt, inits)
+
+            def one_by_one():
+                res["s"] = [cvo.align_batch([a], [b], [T]) for a, b, T in zip(S, Tt, inits)]
+            sec_b = timed(batched)
+            sec_s = timed(one_by_one)
+            Tb, _, itb, _ = res["b"]
+            same = all(np.allclose(Tb[k], r[0][0], atol=1e-6) and int(itb[k]) == int(r[2][0])
+                       for k, r in enumerate(res["s"]))
+            out_legs[name] = {"registrations": len(S), "batched_s": round(sec_b, 4), "one_by_one_s": round(sec_s, 4),
+                              "speedup": round(sec_s / sec_b, 3), "mean_iters": float(np.mean(itb)),
+                              "max_iters": int(np.max(itb)), "identical_results": bool(same)}
+        out.update({"metric": "registrations/s, one persistent batch against one call per registration",
+                    "unit": "registrations/s", "value": round(len(gs) / out_legs["pairs"]["batched_s"], 4),
+                    "legs": out_legs,
+                    "config": {"pairs_points": sizes, "hypotheses_points": args.points, "params": "color.yaml",
+                               "hypotheses": "24-rotation grid, one global pair", "timing": "host clock, synchronised"}})
     elif args.component == "proposal":
         from oracle import proposal as op
         from rkhs_ba_gb300.proposal import ProposalNet, ScenePool
@@ -746,7 +788,7 @@ def main():
     ap.add_argument("--eval-pairs", type=int, default=200, help="held-out pairs of --component global-eval")
     ap.add_argument("--eval-seed0", type=int, default=5000, help="first seed of --component global-eval's pairs")
     ap.add_argument("--component", default="",
-                    choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval"],
+                    choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval", "batching"],
                     help="time one component instead of the main workload")
     args = ap.parse_args()
     from rkhs_ba_gb300 import _build

@@ -220,3 +220,19 @@ def test_global_eval_component_with_a_faked_gpu(tmp_path):
     for m in ("learned", "plain_grid"):
         assert d[m]["value"] > 0 and 0.0 <= d[m]["success_rate"] <= 1.0
     assert d["learned_over_plain_grid"] > 0
+
+
+def test_batching_component_with_a_faked_gpu(tmp_path):
+    """bench.py --component batching (one persistent batch against one call per
+    registration, for uneven pairs and for the 24 grid hypotheses) with the GPU faked."""
+    script = tmp_path / "fake_gpu_bench.py"
+    script.write_text(_FAKE_GPU_CHILD)
+    r = subprocess.run([sys.executable, str(script), ROOT, "--component", "batching", "--pairs", "2", "--points", "2000",
+                        "--steps", "1", "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
+    assert d["component"] == "batching"
+    assert d["legs"]["pairs"]["registrations"] == 2 and d["legs"]["hypotheses"]["registrations"] == 24
+    assert all(20000 <= n <= 60000 for n in d["config"]["pairs_points"])
+    for leg in d["legs"].values():
+        assert leg["speedup"] > 0 and leg["identical_results"] is True
