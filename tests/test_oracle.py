@@ -333,6 +333,18 @@ def test_cpu_inner_product_library_matches_oracle():
     assert orc.function_angle(p, src, src, np.eye(4), 0.3, False, False) == pytest.approx(1.0, rel=1e-5)
 
 
+def test_cpu_inner_product_library_matches_oracle_full_size():
+    """The reference's CPU inner product (radius search, no cap) at the 50,000-point colour
+    size: the library's OpenMP implementation and the oracle agree to 1e-6 relative."""
+    src, tgt, _ = scenes.stereo_pair(n=50000, seed=2)
+    p = CvoParams(params_path("color"))
+    cvo = CvoGPU(params=p)
+    lib_v = cvo.inner_product_cpu(src, tgt, np.eye(4), 0.4)
+    orc_v, _ = orc.inner_product_cpu_semantics(p, src, tgt, np.eye(4), 0.4)
+    assert orc_v > 1e5
+    assert lib_v == pytest.approx(orc_v, rel=1e-6)
+
+
 def test_rotation_grids_are_groups():
     for kind, n in ((0, 60), (1, 24)):
         G = CvoGPU.rotation_grid(kind).astype(np.float64)
