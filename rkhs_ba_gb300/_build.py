@@ -73,7 +73,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc, "-shared", "-Xcompiler", "-fopenmp"] + ARCH + ["-o", tmp] + objs
+    cmd = [nvcc, "-shared", "-Xcompiler", "-fopenmp"] + ARCH + ["-o", tmp] + objs + ["-ldl"]   # NVTX3 loads its tool
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
@@ -120,7 +120,7 @@ def build_sanitized() -> str:
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    cmd = [nvcc, "-shared", "-Xcompiler", "-fopenmp"] + SAN_FLAGS[:4] + ARCH + ["-o", SAN_LIB_PATH] + objs
+    cmd = [nvcc, "-shared", "-Xcompiler", "-fopenmp"] + SAN_FLAGS[:4] + ARCH + ["-o", SAN_LIB_PATH] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

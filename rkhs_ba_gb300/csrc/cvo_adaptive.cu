@@ -259,6 +259,7 @@ bool dalloc(T **p, size_t count) {
 
 int run_association_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell,
                              std::vector<int> *rowptr, std::vector<int> *col, std::vector<float> *val) {
+  NvtxRange nvtx_range("adaptive_association");
   const int n = src->n, m = tgt->n;
   if (src->F != tgt->F || src->C != tgt->C) return CVO_ERR_INVALID_ARG;
   rowptr->assign((size_t)n + 1, 0);
@@ -316,6 +317,7 @@ int run_association_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const floa
 
 int run_align_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const float T_init[16], float T_out[16],
                        double *secs, int *iters_out, double *trace, int trace_len) {
+  NvtxRange nvtx_range("adaptive_align");
   const cvo_params &p = h->params;
   const int n = src->n, m = tgt->n;
   if (src->F != tgt->F || src->C != tgt->C) return CVO_ERR_INVALID_ARG;

@@ -201,6 +201,7 @@ void kernel_inverse3(const float K[9], float Ki[9]) {
 
 int run_association_aniso(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], const float kernel[9],
                           int cap, std::vector<int> *rowptr, std::vector<int> *col, std::vector<float> *val) {
+  NvtxRange nvtx_range("aniso_association");
   const int n = src->n, m = tgt->n;
   if (src->F != tgt->F || src->C != tgt->C) return CVO_ERR_INVALID_ARG;
   rowptr->assign((size_t)n + 1, 0);

@@ -808,6 +808,7 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
                     const std::vector<float> &T_init, BatchResult *res, double *secs, bool export_assoc,
                     std::vector<std::vector<int>> *a_rows, std::vector<std::vector<int>> *a_cols,
                     std::vector<std::vector<float>> *a_vals) {
+  NvtxRange nvtx_range("align_batch");
   const int np = (int)srcs.size();
   if (np == 0) return 0;
   KParams K = make_kparams(h->params);
@@ -920,6 +921,7 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
 // the given poses (inner_product_impl, src/cvo/CvoGPU.cu:1673-1732).
 int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
                             const std::vector<float> &T, float ell, int cap, std::vector<double> *asum) {
+  NvtxRange nvtx_range("inner_product_pairs");
   const int np = (int)srcs.size();
   asum->assign(np, 0.0);
   if (np == 0) return 0;
@@ -937,6 +939,7 @@ int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, cons
 
 int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell, int reps,
                          std::vector<TuneConfig> *configs, std::vector<float> *ms, int *best) {
+  NvtxRange nvtx_range("autotune");
   // candidates: cells of r/2 .. r/6 against the radius, tile-box terms of 4 .. 16 cells
   const float div_r[] = {2.f, 3.f, 4.f, 6.f};
   const float div_ext[] = {4.f, 8.f, 16.f};
@@ -989,6 +992,7 @@ int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[
 int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::vector<float> &T, float ell, int cap,
                             std::vector<double> *asum, std::vector<long long> *nnz, bool export_assoc,
                             std::vector<int> *a_rowptr, std::vector<int> *a_cols, std::vector<float> *a_vals) {
+  NvtxRange nvtx_range("inner_product_batch");
   const int np = (int)(T.size() / 16);
   KParams K = make_kparams(h->params);
   BatchHost bh;
@@ -1012,6 +1016,7 @@ int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const 
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
                           const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out,
                           const KParams *kparams) {
+  NvtxRange nvtx_range("association_edges");
   const int ne = (int)srcs.size();
   out->assign(ne, EdgeAssoc());
   if (ne == 0) return 0;

@@ -115,6 +115,7 @@ __global__ void k_compact_points(int n_sel, int F, int C, const int *flag, const
 int cloud_from_rgbd(Handle *h, const uint8_t *image, int rows, int cols, int channels, const float *depth,
                     const float intrinsic[4], float scaling_factor, const int *uv, int n_sel, const float *geom_type,
                     int num_classes, const float *semantics, DevCloud **out) {
+  NvtxRange nvtx_range("cloud_from_rgbd");
   if (rows < 3 || cols < 3 || (channels != 1 && channels != 3) || n_sel < 0 || num_classes < 0) return CVO_ERR_INVALID_ARG;
   if (!image || !depth || !intrinsic || (n_sel > 0 && !uv) || (num_classes > 0 && !semantics)) return CVO_ERR_INVALID_ARG;
   const size_t total = (size_t)rows * cols;

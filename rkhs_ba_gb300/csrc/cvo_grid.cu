@@ -217,6 +217,7 @@ static void set_extent(DevCloud *d, const float mn[3], const float mx[3], double
 }
 
 int cloud_upload(Handle *h, const cvo_cloud *c, DevCloud **out) {
+  NvtxRange nvtx_range("cloud_upload");
   if (!c || !out) return CVO_ERR_INVALID_ARG;
   if (c->n < 0 || c->F < 0 || c->C < 0) return CVO_ERR_INVALID_ARG;
   if (c->n > 0 && (!c->xyz || (c->xyz_stride != 3 && c->xyz_stride != 4))) return CVO_ERR_INVALID_ARG;

@@ -15,6 +15,7 @@
 #include <vector>
 #include <map>
 #include <new>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/cvo_gb300.h"
 
 namespace cvo_gb {
@@ -313,6 +314,15 @@ int set_cuda_error(Handle *h, cudaError_t e, const char *where);
     cudaError_t e__ = (call);                                      \
     if (e__ != cudaSuccess) return set_cuda_error((h), e__, #call); \
   } while (0)
+
+// NVTX range over a host phase (no-op unless a profiler is attached): ncu can select
+// launches by phase with --nvtx --nvtx-include "<name>/".
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Status of the exception being handled: the C entry points catch everything, so no
 // C++ exception crosses the C ABI (host allocation failure -> out of memory).

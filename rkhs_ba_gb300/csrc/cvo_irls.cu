@@ -339,6 +339,7 @@ int lm_solve(Normal &N, int nf, double *poses, const uint8_t *hold, int max_iter
 
 int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, const uint8_t *hold, int ne,
                     const int *edges, double *secs, int *iters) {
+  NvtxRange nvtx_range("align_multi");
   auto t0 = std::chrono::steady_clock::now();
   const cvo_params &p = h->params;
   if (p.multiframe_is_optimizing_ell) return CVO_ERR_UNSUPPORTED;

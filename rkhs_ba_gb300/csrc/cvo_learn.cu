@@ -568,6 +568,7 @@ int net_points(const NetDev *n) { return n->P; }
 // Forward pass over the 2 Bn slots (pair b: source slot 2b, target slot 2b + 1):
 // outputs in n->O, centroids of the moved clouds in n->cent.
 static int net_forward(Handle *h, NetDev *n, int Bn, const std::vector<NetSlot> &slots, uint32_t seed) {
+  NvtxRange nvtx_range("proposal_forward");
   int rc = net_ensure(h, n, Bn);
   if (rc) return rc;
   const int S = 2 * Bn, P = n->P;
@@ -662,6 +663,7 @@ int net_hypotheses(Handle *h, NetDev *n, int Bn, DevCloud *const *src, DevCloud 
 // lr > 0 also one Adam step.  T_label: row-major 3x4 per pair (target = T source).
 int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *src, const float *tgt, int Bn,
                    const int *scene, const float *T_label, float lr, uint32_t seed, float *loss_out) {
+  NvtxRange nvtx_range("proposal_train");
   int rc = check_pool_args(n_scenes, n_pts, src, tgt, Bn, scene);
   if (rc) return rc;
   if (!T_label || !(lr >= 0.f)) return CVO_ERR_INVALID_ARG;
