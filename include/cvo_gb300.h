@@ -403,6 +403,17 @@ int cvo_register_learned_batch_dev(cvo_handle *h, cvo_proposal *p, int n_pairs, 
                                    float fallback_cos, float refine_ell, uint32_t seed, float *T_out,
                                    float *cos_out, int *used_fallback, int *iters, double *secs);
 
+/* Global registration of n_pairs host pairs in one call (poses in cvo_align's T_out
+ * convention, n_pairs x 16; iters n_pairs ints, may be NULL).  use_learned = 0: the
+ * plain grid, CvoGPU::get_nearest_init_pose (src/cvo/CvoGPU.cpp:367-398) over the 24
+ * cube rotations at ell_init_first_frame, then align from the inverted grid pose as
+ * CvoGPU::align's int overload does (src/cvo/CvoGPU.cu:1533-1543), all pairs in one
+ * batched align.  use_learned = 1: cvo_register_learned_batch_dev with proposal (best 2
+ * of 8 hypotheses refined, ranked and judged at ell_init_first_frame, grid fallback
+ * below cos-angle 0).  No reference counterpart as one call. */
+int cvo_global_register(cvo_handle *h, int n_pairs, const cvo_cloud *srcs, const cvo_cloud *tgts,
+                        int use_learned, cvo_proposal *proposal, float *T_out, int *iters, double *secs);
+
 /* ---------------------------------------------------------- multi-frame */
 /* CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670)
  * -> CvoBatchIRLS::solve (src/cvo/IRLS.cpp:148-367).  poses: n_frames*12 doubles

@@ -125,6 +125,7 @@ SIGNATURES = {
     "cvo_proposal_hypotheses_dev": (_i, [_P, _P, _i, C.POINTER(_P), C.POINTER(_P), C.c_uint32, _FP]),
     "cvo_register_learned_batch_dev": (_i, [_P, _P, _i, C.POINTER(_P), C.POINTER(_P), _i, _f, _f, _f, _f,
                                             C.c_uint32, _FP, _FP, _IP, _IP, _DP]),
+    "cvo_global_register": (_i, [_P, _i, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _i, _P, _FP, _IP, _DP]),
     "cvo_align_multi": (_i, [_P, _i, C.POINTER(CvoCloudC), _DP, C.POINTER(C.c_uint8), _i, _IP, _DP, _IP]),
     "cvo_align_multi_dev": (_i, [_P, _i, C.POINTER(_P), _DP, C.POINTER(C.c_uint8), _i, _IP, _DP, _IP]),
     "cvo_status_string": (C.c_char_p, [_i]),

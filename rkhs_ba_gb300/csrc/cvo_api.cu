@@ -1391,6 +1391,50 @@ extern "C" int cvo_register_learned_batch_dev(cvo_handle *H, cvo_proposal *p, in
   return status_from_exception();
 }
 
+// ---------------------------------------------------- global registration
+// Host pairs in, poses out: the plain grid (the reference's get_nearest_init_pose over
+// the 24 cube rotations, then align from the inverted grid pose as the int overload of
+// CvoGPU::align does, src/cvo/CvoGPU.cu:1533-1543), every pair in one batched align; or
+// the learned proposal with the Python binding's defaults (best 2 hypotheses refined,
+// ranked and judged at ell_init_first_frame, grid fallback below cos-angle 0).
+extern "C" int cvo_global_register(cvo_handle *H, int n_pairs, const cvo_cloud *srcs, const cvo_cloud *tgts,
+                                   int use_learned, cvo_proposal *proposal, float *T_out, int *iters,
+                                   double *secs) try {
+  if (!H || n_pairs < 0 || (n_pairs > 0 && (!srcs || !tgts || !T_out)) || (use_learned && !proposal))
+    return CVO_ERR_INVALID_ARG;
+  if (secs) *secs = 0;
+  if (n_pairs == 0) return CVO_OK;
+  if (!H->h.stream) return CVO_ERR_CUDA;
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<cvo_gpu_cloud *> s(n_pairs, nullptr), t(n_pairs, nullptr);
+  int rc = 0;
+  for (int b = 0; b < n_pairs && !rc; b++) {
+    rc = cvo_cloud_upload(H, &srcs[b], &s[b]);
+    if (!rc) rc = cvo_cloud_upload(H, &tgts[b], &t[b]);
+  }
+  const float ell = H->h.params.ell_init_first_frame;
+  if (!rc && use_learned) {
+    rc = cvo_register_learned_batch_dev(H, proposal, n_pairs, s.data(), t.data(), 2, ell, ell, 0.f, 0.f, 0u, T_out,
+                                        nullptr, nullptr, iters, nullptr);
+  } else if (!rc) {
+    std::vector<float> inits(16 * (size_t)n_pairs);
+    for (int b = 0; b < n_pairs && !rc; b++) {
+      float g[16];
+      rc = cvo_get_nearest_init_pose_dev(H, s[b], t[b], ell, 0, 1, g, nullptr);
+      if (!rc) rigid_inverse(g, &inits[16 * (size_t)b]);
+    }
+    if (!rc) rc = cvo_align_batch_dev(H, n_pairs, s.data(), t.data(), inits.data(), T_out, nullptr, iters, nullptr);
+  }
+  for (cvo_gpu_cloud *c : s)
+    if (c) cvo_cloud_free(H, c);
+  for (cvo_gpu_cloud *c : t)
+    if (c) cvo_cloud_free(H, c);
+  if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+} catch (...) {
+  return status_from_exception();
+}
+
 // ------------------------------------------------------------ multi-frame
 extern "C" int cvo_align_multi_dev(cvo_handle *H, int n_frames, cvo_gpu_cloud *const *clouds, double *poses,
                                    const uint8_t *hold_const, int n_edges, const int *edges, double *secs,

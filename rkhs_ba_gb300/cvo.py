@@ -443,6 +443,25 @@ class CvoGPU:
                 "cvo_register_learned_batch_dev", self._h)
         return [_from16(To[16 * i:16 * i + 16]) for i in range(n)], cos, fb, its, secs.value
 
+    def global_register(self, sources, targets, net=None):
+        """cvo_global_register: host pairs in, poses out in one call.  Without net the
+        plain grid (nearest of the 24 cube rotations, then one batched align); with net
+        the learned proposal (register_learned_batch's defaults).  Returns (list of 4x4
+        in align's output convention, iterations (n,), seconds)."""
+        n = len(sources)
+        if len(targets) != n:
+            raise ValueError("one target per source")
+        cs = (L.CvoCloudC * max(n, 1))(*[c.c_struct() for c in sources])
+        ct = (L.CvoCloudC * max(n, 1))(*[c.c_struct() for c in targets])
+        To = np.zeros(16 * max(n, 1), np.float32)
+        its = np.zeros(max(n, 1), np.int32)
+        secs = C.c_double(0)
+        L.check(L.lib().cvo_global_register(self._h, n, cs, ct, 0 if net is None else 1,
+                                            None if net is None else net.handle, To.ctypes.data_as(_FP),
+                                            its.ctypes.data_as(C.POINTER(C.c_int)), C.byref(secs)),
+                "cvo_global_register", self._h)
+        return [_from16(To[16 * i:16 * i + 16]) for i in range(n)], its[:n], secs.value
+
     # -- autotuner -----------------------------------------------------
     def autotune(self, source: GpuCloud, target: GpuCloud, T=None, ell: float = 0.0, reps: int = 3) -> dict:
         """Times the association's cell-size configurations on one pair and keeps the fastest

@@ -248,3 +248,28 @@ def test_host_allocation_failure_returns_a_status():
     r = subprocess.run([sys.executable, "-c", _OOM_CHILD, ROOT], capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     assert int(r.stdout.strip().splitlines()[-1]) == L.CVO_ERR_OUT_OF_MEMORY
+
+
+def test_global_register_host_checks():
+    """cvo_global_register: argument checks and the no-GPU status, on the host."""
+    cvo = CvoGPU(params=CvoParams())
+    a = CvoPointCloud(np.random.default_rng(1).uniform(-1, 1, (60, 3)))
+    T = np.zeros(16, np.float32)
+    lib = L.lib()
+    S = (L.CvoCloudC * 1)(a.c_struct())
+    assert lib.cvo_global_register(cvo._h, 0, None, None, 0, None, None, None, None) == L.CVO_OK
+    assert lib.cvo_global_register(cvo._h, 1, S, S, 1, None, T.ctypes.data_as(C.POINTER(C.c_float)), None,
+                                   None) == L.CVO_ERR_INVALID_ARG          # learned without a proposal
+    assert lib.cvo_global_register(cvo._h, -1, S, S, 0, None, T.ctypes.data_as(C.POINTER(C.c_float)), None,
+                                   None) == L.CVO_ERR_INVALID_ARG
+    with pytest.raises(ValueError):
+        cvo.global_register([a], [])
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(L.CvoError) as e:
+            cvo.global_register([a], [a])
+        assert e.value.code == L.CVO_ERR_CUDA
