@@ -161,28 +161,6 @@ def test_trained_network_gain_over_the_grid(cvo, trained):
     assert fb.sum() <= 2
 
 
-def test_global_register_equals_the_calls_it_composes(cvo, trained):
-    """cvo_global_register (host pairs in, poses out) gives exactly what its parts give:
-    the plain grid (nearest of the 24 rotations, inverted, one batched align) and the
-    learned registration with register_learned_batch's defaults."""
-    net = trained[0]
-    pairs = [scenes.global_pair(n=6000, seed=4_100_000 + k) for k in range(3)]
-    srcs = [s for s, _, _ in pairs]
-    tgts = [t for _, t, _ in pairs]
-    gs = [cvo.upload(s) for s in srcs]
-    gt = [cvo.upload(t) for t in tgts]
-    p = cvo.get_params()
-    T_g, it_g, _ = cvo.global_register(srcs, tgts)
-    inits = [scenes.inv_T(cvo.get_nearest_init_pose(s, t, p.ell_init_first_frame, 0, 1)[0]) for s, t in zip(gs, gt)]
-    Tp, _, itp, _ = cvo.align_batch(gs, gt, inits)
-    for k in range(len(pairs)):
-        assert np.array_equal(T_g[k], Tp[k]) and it_g[k] == itp[k], k
-    T_l, it_l, _ = cvo.global_register(srcs, tgts, net)
-    Tr, _, _, itr, _ = cvo.register_learned_batch(net, gs, gt)
-    for k in range(len(pairs)):
-        assert np.array_equal(T_l[k], Tr[k]) and it_l[k] == itr[k], k
-
-
 def test_invalid_arguments_are_rejected(cvo, small_pool):
     from rkhs_ba_gb300._lib import CvoError
     from rkhs_ba_gb300 import CvoPointCloud
