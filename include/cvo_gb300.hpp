@@ -166,6 +166,28 @@ class CvoGPU {
     return T;
   }
 
+  /* Global registration of host pairs in one call (cvo_global_register): the plain grid
+   * (nearest of the 24 cube rotations, then one batched align), or the learned proposal
+   * when proposal is non-null.  Poses in align's T_out convention. */
+  std::vector<Mat4> global_register(const std::vector<PointCloud> &sources, const std::vector<PointCloud> &targets,
+                                    cvo_proposal *proposal = nullptr, std::vector<int> *iters = nullptr,
+                                    double *seconds = nullptr) const {
+    if (sources.size() != targets.size())
+      throw Error(CVO_ERR_INVALID_ARG, "global_register: one target per source");
+    std::vector<cvo_cloud> s, t;
+    for (size_t k = 0; k < sources.size(); k++) {
+      s.push_back(sources[k].view());
+      t.push_back(targets[k].view());
+    }
+    std::vector<Mat4> T(sources.size());
+    std::vector<int> it(sources.size(), 0);
+    check(cvo_global_register(h_, (int)sources.size(), s.data(), t.data(), proposal ? 1 : 0, proposal,
+                              T.empty() ? nullptr : T[0].data(), it.data(), seconds),
+          "cvo_global_register", h_);
+    if (iters) *iters = it;
+    return T;
+  }
+
   /* CvoGPU::align(frames, frames_to_hold_const, edges, secs) (src/cvo/CvoGPU.cu:1615-1670):
    * poses n_frames x 12 doubles (row-major [R|t], frame -> world), updated in place. */
   int align(const std::vector<PointCloud> &frames, std::vector<std::array<double, 12>> &poses,

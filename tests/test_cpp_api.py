@@ -27,9 +27,10 @@ using namespace cvo_gb300;
 static int fail(int code, const char *what) { std::fprintf(stderr, "FAIL %d: %s\n", code, what); return code; }
 
 int main(int argc, char **argv) {
+  if (argc < 2) return fail(20, "usage: client params.yaml");
   const std::string yaml = argv[1];
-  const bool has_gpu = argc > 2 && std::string(argv[2]) == "gpu";
   CvoGPU cvo(yaml);
+  const bool has_gpu = cvo_get_stream(cvo.handle()) != nullptr;   // a handle made without a CUDA device has none
   cvo_params p = cvo.get_params();
   const float ell0 = p.ell_init;
   p.ell_init = 0.25f;
@@ -76,7 +77,20 @@ int main(int argc, char **argv) {
     } catch (const Error &e) {
       if (e.code != CVO_ERR_CUDA) return fail(10, "no-GPU status");
     }
+    try {
+      cvo.global_register({a}, {a});
+      return fail(15, "global registration without a GPU");
+    } catch (const Error &e) {
+      if (e.code != CVO_ERR_CUDA) return fail(16, "no-GPU status of global_register");
+    }
   }
+  try {
+    cvo.global_register({a, a}, {a});
+    return fail(17, "mismatched pairs accepted");
+  } catch (const Error &e) {
+    if (e.code != CVO_ERR_INVALID_ARG) return fail(18, "mismatched pairs status");
+  }
+  if (!cvo.global_register({}, {}).empty()) return fail(19, "no pairs");
 
   // pose graph: a chain with a prior recovers the odometry
   PoseGraphSolver g;
@@ -104,14 +118,6 @@ int main(int argc, char **argv) {
 """
 
 
-def _has_gpu():
-    try:
-        import torch
-        return bool(torch.cuda.is_available())
-    except Exception:
-        return False
-
-
 def test_cpp_client_of_the_cvogpu_mirror():
     lib_dir = os.path.dirname(L.LIB_PATH)
     inc = os.path.join(ROOT, "include")
@@ -121,8 +127,7 @@ def test_cpp_client_of_the_cvogpu_mirror():
         exe = os.path.join(d, "client")
         subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I" + inc, src, "-o", exe,
                         "-L" + lib_dir, "-lcvo_gb300", "-Wl,-rpath," + lib_dir], check=True)
-        r = subprocess.run([exe, params_path("geometric"), "gpu" if _has_gpu() else "cpu"], capture_output=True,
-                           text=True, timeout=300)
+        r = subprocess.run([exe, params_path("geometric")], capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
         assert r.stdout.startswith("ok ")
 
