@@ -225,6 +225,37 @@ class CvoGPU {
   cvo_handle *h_ = nullptr;
 };
 
+/* cvo::AdaptiveCvoGPU (include/UnifiedCvo/cvo/AdaptiveCvoGPU.hpp:161-180): CVO whose
+ * lengthscale follows the gradient of the inner product (src/cvo/AdaptiveCvoGPU.cu:1077-1250). */
+class AdaptiveCvoGPU {
+ public:
+  explicit AdaptiveCvoGPU(const std::string &param_file) { check(cvo_create(param_file.c_str(), &h_), "cvo_create"); }
+  explicit AdaptiveCvoGPU(const cvo_params &params) {
+    check(cvo_create_with_params(&params, &h_), "cvo_create_with_params");
+  }
+  ~AdaptiveCvoGPU() {
+    if (h_) cvo_destroy(h_);
+  }
+  AdaptiveCvoGPU(const AdaptiveCvoGPU &) = delete;
+  AdaptiveCvoGPU &operator=(const AdaptiveCvoGPU &) = delete;
+  cvo_handle *handle() const { return h_; }
+
+  /* AdaptiveCvoGPU::align(source, target, init_guess_transform, transform, registration_seconds)
+   * (AdaptiveCvoGPU.hpp:171-175): 0, or -1 on a zero gradient; an empty cloud throws
+   * (CVO_ERR_EMPTY_CLOUD). */
+  int align(const PointCloud &source, const PointCloud &target, const Mat4 &init_guess_transform, Mat4 &transform,
+            double *registration_seconds = nullptr, int *num_iters = nullptr) const {
+    const cvo_cloud s = source.view(), t = target.view();
+    const int rc = cvo_align_adaptive(h_, &s, &t, init_guess_transform.data(), transform.data(),
+                                      registration_seconds, num_iters);
+    check(rc, "cvo_align_adaptive", h_);
+    return rc == CVO_ZERO_GRADIENT ? -1 : 0;
+  }
+
+ private:
+  cvo_handle *h_ = nullptr;
+};
+
 /* The keyframe pose graph's solver (GTSAM's Prior / Between Pose3 factors of
  * src/graph_optimizer/PoseGraph.cpp:321-495): poses row-major double[12]; sigmas
  * rotation first, as in GTSAM. */

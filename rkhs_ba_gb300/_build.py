@@ -35,11 +35,13 @@ def _sources() -> list[str]:
 
 
 def _digest() -> str:
+    """Hash of what the library is compiled from: the CUDA sources and the C headers
+    (the header-only C++ mirror, include/*.hpp, is not part of the library)."""
     h = hashlib.sha256()
     for d in (CSRC, os.path.join(ROOT, "include")):
         for f in sorted(os.listdir(d)):
             p = os.path.join(d, f)
-            if os.path.isfile(p):
+            if os.path.isfile(p) and not f.endswith(".hpp"):
                 h.update(f.encode())
                 with open(p, "rb") as fh:
                     h.update(fh.read())

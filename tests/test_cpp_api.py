@@ -3,7 +3,8 @@ built with -Wall -Wextra -Werror links the library and runs the host paths the w
 reference user would call them: construction from a parameter file, parameters read
 and written back, the CPU inner product and cos-angle, empty-input returns, errors as
 exceptions carrying the status, the multi-frame argument checks and the pose-graph
-solver.  On a machine without a GPU the GPU methods must throw the CUDA status."""
+solver, the adaptive-lengthscale class.  On a machine without a GPU the GPU methods must
+throw the CUDA status."""
 import os
 import subprocess
 import tempfile
@@ -91,6 +92,14 @@ int main(int argc, char **argv) {
     if (e.code != CVO_ERR_INVALID_ARG) return fail(18, "mismatched pairs status");
   }
   if (!cvo.global_register({}, {}).empty()) return fail(19, "no pairs");
+  AdaptiveCvoGPU acvo(yaml);
+  try {
+    Mat4 T2{};
+    acvo.align(empty, a, I, T2);
+    return fail(21, "adaptive align of an empty cloud accepted");
+  } catch (const Error &e) {
+    if (e.code != CVO_ERR_EMPTY_CLOUD) return fail(22, "adaptive empty-cloud status");
+  }
 
   // pose graph: a chain with a prior recovers the odometry
   PoseGraphSolver g;
