@@ -1,5 +1,6 @@
-"""GPU checks of the entry points added on top of the engine, run last so that a
-failure here cannot hide the results of the kernel parity tests:
+"""GPU checks of the entry points added on top of the engine.  The file sorts after
+every kernel-parity file (test_gpu_*), so that under ``pytest -x`` a failure here
+cannot hide the results of those tests:
 
 * the C++ mirror (include/cvo_gb300.hpp) registers and computes inner products exactly
   as the Python binding does;
@@ -38,6 +39,7 @@ static PointCloud read_cloud(std::ifstream &in) {
 }
 
 int main(int argc, char **argv) {
+  if (argc < 3) return 2;
   std::ifstream in(argv[2], std::ios::binary);
   PointCloud src = read_cloud(in), tgt = read_cloud(in);
   CvoGPU cvo(argv[1]);
