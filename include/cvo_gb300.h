@@ -238,8 +238,10 @@ int cvo_inner_product_batch_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud
  * the result (same semantics as cvo_inner_product) is written to the device
  * float *out_dev on `cuda_stream` (NULL = default stream); the call does not
  * synchronize.  Its only scratch is a fixed 65,792-byte array inside this
- * library, so at most 1,048,576 source points per call (else
- * CVO_ERR_CAPACITY); it costs O(N * M).  All calls share that array: calls
+ * library, so at most 1,048,576 source points per call; it scans every target
+ * for every source row (O(N * M)), so N * M is limited to 2^33 pair tests per
+ * call (about 92k x 92k points; larger calls return CVO_ERR_CAPACITY before
+ * touching the device).  All calls share that array: calls
  * whose kernels overlap on the GPU race and must be ordered by the caller.  The
  * first call on a device looks the array up with that device current; make it
  * before any stream capture.  No handle is needed. */

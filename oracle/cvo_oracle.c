@@ -1315,46 +1315,91 @@ typedef struct {
   float *a;              /* kernel values */
 } res_edge;
 
+/* Residual k of the edges' flattened residual list: cost term, and with want the
+ * Jacobian row (12 entries) and r.  Returns the residual's cost 1/2 r^2. */
+static double lm_residual(const double *poses, const res_edge *Ee, int k, int want, double J[12], double *rr_out) {
+  const double *T1 = poses + 12 * Ee->f1, *T2 = poses + 12 * Ee->f2;
+  double p1[3] = {Ee->p1[3 * k], Ee->p1[3 * k + 1], Ee->p1[3 * k + 2]};
+  double p2[3] = {Ee->p2[3 * k], Ee->p2[3 * k + 1], Ee->p2[3 * k + 2]};
+  double q1[3], q2[3], ev[3];
+  for (int r = 0; r < 3; r++) {
+    q1[r] = T1[4 * r] * p1[0] + T1[4 * r + 1] * p1[1] + T1[4 * r + 2] * p1[2] + T1[4 * r + 3];
+    q2[r] = T2[4 * r] * p2[0] + T2[4 * r + 1] * p2[1] + T2[4 * r + 2] * p2[2] + T2[4 * r + 3];
+    ev[r] = q1[r] - q2[r];
+  }
+  double a = Ee->a[k];
+  double rr = a * (ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+  *rr_out = rr;
+  if (want) {
+    double u1[3], u2[3];
+    for (int r = 0; r < 3; r++) {
+      u1[r] = T1[r] * ev[0] + T1[4 + r] * ev[1] + T1[8 + r] * ev[2];  /* R1^T e */
+      u2[r] = T2[r] * ev[0] + T2[4 + r] * ev[1] + T2[8 + r] * ev[2];  /* R2^T e */
+    }
+    J[0] = u1[0]; J[1] = u1[1]; J[2] = u1[2];
+    J[3] = p1[1] * u1[2] - p1[2] * u1[1]; J[4] = p1[2] * u1[0] - p1[0] * u1[2]; J[5] = p1[0] * u1[1] - p1[1] * u1[0];
+    J[6] = -u2[0]; J[7] = -u2[1]; J[8] = -u2[2];
+    J[9] = -(p2[1] * u2[2] - p2[2] * u2[1]); J[10] = -(p2[2] * u2[0] - p2[0] * u2[2]); J[11] = -(p2[0] * u2[1] - p2[1] * u2[0]);
+  }
+  return 0.5 * rr * rr;
+}
+
+/* Cost 1/2 sum r^2 and (with want) the normal equations H = sum J^T J, g = sum J^T r.
+ * Each edge's residuals are split into fixed chunks of kLmChunk; every chunk is summed
+ * in residual order and the chunks are added in edge / chunk order, so the result does
+ * not depend on the number of threads.  Per residual only the 78 terms of the upper
+ * triangle of its 12 x 12 block are accumulated; the lower triangle is mirrored. */
+#define LM_CHUNK 4096
 static void lm_eval(int nf, const double *poses, int ne, const res_edge *E, int want, double *H, double *g,
                     double *cost) {
   int D = 6 * nf;
-  if (want) { memset(H, 0, sizeof(double) * (size_t)D * D); memset(g, 0, sizeof(double) * D); }
-  double c = 0.0;
-  for (int e = 0; e < ne; e++) {
-    const double *T1 = poses + 12 * E[e].f1, *T2 = poses + 12 * E[e].f2;
-    for (int k = 0; k < E[e].n; k++) {
-      double p1[3] = {E[e].p1[3 * k], E[e].p1[3 * k + 1], E[e].p1[3 * k + 2]};
-      double p2[3] = {E[e].p2[3 * k], E[e].p2[3 * k + 1], E[e].p2[3 * k + 2]};
-      double q1[3], q2[3], ev[3];
-      for (int r = 0; r < 3; r++) {
-        q1[r] = T1[4 * r] * p1[0] + T1[4 * r + 1] * p1[1] + T1[4 * r + 2] * p1[2] + T1[4 * r + 3];
-        q2[r] = T2[4 * r] * p2[0] + T2[4 * r + 1] * p2[1] + T2[4 * r + 2] * p2[2] + T2[4 * r + 3];
-        ev[r] = q1[r] - q2[r];
-      }
-      double a = E[e].a[k];
-      double rr = a * (ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
-      c += 0.5 * rr * rr;
+  long long nchunks = 0;
+  for (int e = 0; e < ne; e++) nchunks += (E[e].n + LM_CHUNK - 1) / LM_CHUNK;
+  const int stride = 1 + 12 + 78;             /* cost, g block, upper-triangle H block */
+  double *part = (double *)calloc((size_t)(nchunks > 0 ? nchunks : 1) * stride, sizeof(double));
+  int *ch_edge = (int *)malloc(sizeof(int) * (size_t)(nchunks > 0 ? nchunks : 1));
+  int *ch_k0 = (int *)malloc(sizeof(int) * (size_t)(nchunks > 0 ? nchunks : 1));
+  {
+    long long q = 0;
+    for (int e = 0; e < ne; e++)
+      for (int k0 = 0; k0 < E[e].n; k0 += LM_CHUNK) { ch_edge[q] = e; ch_k0[q] = k0; q++; }
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long long q = 0; q < nchunks; q++) {
+    const res_edge *Ee = &E[ch_edge[q]];
+    double *pc = part + (size_t)q * stride;
+    int k1 = ch_k0[q] + LM_CHUNK < Ee->n ? ch_k0[q] + LM_CHUNK : Ee->n;
+    for (int k = ch_k0[q]; k < k1; k++) {
+      double J[12], rr;
+      pc[0] += lm_residual(poses, Ee, k, want, J, &rr);
       if (!want) continue;
-      double u1[3], u2[3], J[12];
-      for (int r = 0; r < 3; r++) {
-        u1[r] = T1[r] * ev[0] + T1[4 + r] * ev[1] + T1[8 + r] * ev[2];  /* R1^T e */
-        u2[r] = T2[r] * ev[0] + T2[4 + r] * ev[1] + T2[8 + r] * ev[2];  /* R2^T e */
-      }
-      J[0] = u1[0]; J[1] = u1[1]; J[2] = u1[2];
-      J[3] = p1[1] * u1[2] - p1[2] * u1[1]; J[4] = p1[2] * u1[0] - p1[0] * u1[2]; J[5] = p1[0] * u1[1] - p1[1] * u1[0];
-      J[6] = -u2[0]; J[7] = -u2[1]; J[8] = -u2[2];
-      J[9] = -(p2[1] * u2[2] - p2[2] * u2[1]); J[10] = -(p2[2] * u2[0] - p2[0] * u2[2]); J[11] = -(p2[0] * u2[1] - p2[1] * u2[0]);
-      int off[2] = {6 * E[e].f1, 6 * E[e].f2};
+      int t = 13;
       for (int a1 = 0; a1 < 12; a1++) {
-        int ia = off[a1 / 6] + a1 % 6;
-        g[ia] += J[a1] * rr;
-        for (int b1 = 0; b1 < 12; b1++) {
-          int ib = off[b1 / 6] + b1 % 6;
-          H[(size_t)ia * D + ib] += J[a1] * J[b1];
-        }
+        pc[1 + a1] += J[a1] * rr;
+        for (int b1 = a1; b1 < 12; b1++) pc[t++] += J[a1] * J[b1];
       }
     }
   }
+  if (want) { memset(H, 0, sizeof(double) * (size_t)D * D); memset(g, 0, sizeof(double) * D); }
+  double c = 0.0;
+  for (long long q = 0; q < nchunks; q++) {
+    const double *pc = part + (size_t)q * stride;
+    const res_edge *Ee = &E[ch_edge[q]];
+    c += pc[0];
+    if (!want) continue;
+    int off[2] = {6 * Ee->f1, 6 * Ee->f2};
+    int t = 13;
+    for (int a1 = 0; a1 < 12; a1++) {
+      int ia = off[a1 / 6] + a1 % 6;
+      g[ia] += pc[1 + a1];
+      for (int b1 = a1; b1 < 12; b1++, t++) {
+        int ib = off[b1 / 6] + b1 % 6;
+        H[(size_t)ia * D + ib] += pc[t];
+        if (ib != ia) H[(size_t)ib * D + ia] += pc[t];
+      }
+    }
+  }
+  free(part); free(ch_edge); free(ch_k0);
   *cost = c;
 }
 

@@ -12,8 +12,9 @@
 // scans the targets in ascending index and keeps the first nearest_neighbors_max
 // pairs whose kernel value exceeds sp_thres -- the set the reference's
 // fill_in_A_mat_gpu keeps (src/cvo/CvoGPU.cu:994-1075) -- so it needs no spatial
-// grid (building one would allocate).  It costs O(N * M) and is meant for
-// moderate cloud sizes.
+// grid (building one would allocate).  It costs O(N * M) pair tests, so a call
+// is also limited to kNoAllocMaxPairTests (N * M <= 2^33, e.g. 92k x 92k
+// points), which keeps one launch well under a few seconds on a GB300.
 //
 // Limits and sharing: at most kNoAllocMaxRows source points per call.  All
 // calls in the process share the one scratch array and leave their partial sums
@@ -35,6 +36,7 @@ constexpr int kNoAllocThreads = 128;
 constexpr int kNoAllocMaxBlocks = 8192;
 constexpr int kNoAllocMaxRows = kNoAllocThreads * kNoAllocMaxBlocks;   // 1,048,576 source points
 constexpr int kNoAllocMaxDevices = 64;
+constexpr long long kNoAllocMaxPairTests = 1LL << 33;                   // N * M per call
 
 // [0, 256): completion counter (unsigned int); [256, ...): one double per block
 constexpr size_t kScratchBytes = 256 + sizeof(double) * kNoAllocMaxBlocks;   // 65,792 bytes
@@ -187,6 +189,7 @@ extern "C" int cvo_inner_product_noalloc(const cvo_params *p, const cvo_cloud *s
   if (src_dev->n < 0 || tgt_dev->n < 0 || src_dev->F != tgt_dev->F || src_dev->C != tgt_dev->C)
     return CVO_ERR_INVALID_ARG;
   if (src_dev->n > kNoAllocMaxRows) return CVO_ERR_CAPACITY;   // more rows than the scratch array serves
+  if ((long long)src_dev->n * (long long)tgt_dev->n > kNoAllocMaxPairTests) return CVO_ERR_CAPACITY;
   if ((src_dev->n > 0 && !src_dev->xyz) || (tgt_dev->n > 0 && !tgt_dev->xyz)) return CVO_ERR_INVALID_ARG;
   if ((src_dev->xyz_stride != 3 && src_dev->xyz_stride != 4) || (tgt_dev->xyz_stride != 3 && tgt_dev->xyz_stride != 4))
     return CVO_ERR_INVALID_ARG;

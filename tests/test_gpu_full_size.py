@@ -11,12 +11,15 @@ with a grid and runs on all host threads):
   lengthscale 1.0).
 
 Column sets bit-exact and values within 1e-5 relative (the bar of the smaller parity
-cases), and the GPU inner product equal to the oracle's within 1e-5 relative.
+cases), and the GPU inner product equal to the oracle's within 1e-5 relative.  The
+library reads the parameter file with its own reader and the oracle with its own
+(oracle/params.py), so the two sides share no parser.
 """
 import numpy as np
 import pytest
 
 from oracle import oracle as orc
+from oracle.params import OracleParams
 from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path, scenes
 
 pytestmark = pytest.mark.gpu
@@ -32,10 +35,11 @@ def _ell_to_csr(ind, val, nnz):
     return row_ptr, ind[used], val[used]
 
 
-def _check(params, src, tgt, T, ell):
-    cvo = CvoGPU(params=params)
+def _check(name, src, tgt, T, ell):
+    cvo = CvoGPU(params=CvoParams(params_path(name)))
+    oparams = OracleParams(params_path(name))
     a = cvo.compute_association_gpu(src, tgt, T, ell)
-    ind, val, nnz = orc.association(params, src, tgt, T, ell)
+    ind, val, nnz = orc.association(oparams, src, tgt, T, ell)
     row_ptr, col, v = _ell_to_csr(ind, val, nnz)
     assert a.rows == src.num_points()
     assert np.array_equal(np.asarray(a.row_ptr, np.int64), row_ptr)
@@ -45,27 +49,26 @@ def _check(params, src, tgt, T, ell):
     bad = np.abs(gv - ov) > REL * np.abs(ov)
     assert not bad.any(), (int(bad.sum()), np.nonzero(bad)[0][:5])
     g = cvo.inner_product_gpu(src, tgt, T, ell)
-    o, _ = orc.inner_product_gpu_semantics(params, src, tgt, T, ell)
+    o, _ = orc.inner_product_gpu_semantics(oparams, src, tgt, T, ell)
     assert g == pytest.approx(o, rel=REL)
     return nnz
 
 
 def test_full_size_geometric_10k(cuda_device):
     src, tgt, _ = scenes.room_pair(n=10000, seed=1)
-    nnz = _check(CvoParams(params_path("geometric")), src, tgt, np.eye(4, dtype=np.float32), 0.25)
+    nnz = _check("geometric", src, tgt, np.eye(4, dtype=np.float32), 0.25)
     assert nnz.sum() > 50000
 
 
 def test_full_size_colour_50k(cuda_device):
     src, tgt, _ = scenes.stereo_pair(n=50000, seed=2)
-    p = CvoParams(params_path("color"))
-    nnz = _check(p, src, tgt, np.eye(4, dtype=np.float32), 0.4)
+    nnz = _check("color", src, tgt, np.eye(4, dtype=np.float32), 0.4)
     assert nnz.sum() > 4_000_000
-    assert (nnz == p.nearest_neighbors_max).sum() > 10000       # the capped-row selection ran
+    cap = OracleParams(params_path("color")).nearest_neighbors_max
+    assert (nnz == cap).sum() > 10000          # the capped-row selection ran
 
 
 def test_full_size_semantic_lidar_128k(cuda_device):
     src, tgt, _ = scenes.lidar_pair(n=128000, seed=1)
-    p = CvoParams(params_path("lidar_semantic"))
-    nnz = _check(p, src, tgt, np.eye(4, dtype=np.float32), 1.0)
+    nnz = _check("lidar_semantic", src, tgt, np.eye(4, dtype=np.float32), 1.0)
     assert nnz.sum() > 1_000_000

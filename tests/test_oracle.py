@@ -9,6 +9,7 @@ import pytest
 import scipy.linalg as sla
 
 from oracle import oracle as orc
+from oracle.params import OracleParams, ParamsC, read_yaml_dict
 from rkhs_ba_gb300 import CvoGPU, CvoParams, CvoPointCloud, params_path, scenes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -359,18 +360,18 @@ def test_rotation_grids_are_groups():
     assert CvoGPU.rotation_grid(2, 3).shape == (27, 3, 3)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/src/cvo/CvoGPU.cpp"), reason="reference sources not mounted")
 def test_icosahedral_grid_equals_reference_set():
     """The 60 rotations regenerated from the icosahedral symmetry are the set that
-    gen_icosahedron_init_rots (src/cvo/CvoGPU.cpp:279-342) lists (as a set, to float rounding)."""
-    import re
-    txt = open("/root/reference/src/cvo/CvoGPU.cpp").read()
-    ref = [np.array([float(v) for v in m.group(1).split(",")]).reshape(3, 3)
-           for m in re.finditer(r"pose\[\d+\]<<([^;]+);", txt)]
+    gen_icosahedron_init_rots (src/cvo/CvoGPU.cpp:279-342) lists (as a set, to float
+    rounding); the reference's table is the fixture tests/golden/icosahedral_rotations.npz
+    written by tests/golden/make_golden.py."""
+    ref = np.load(os.path.join(GOLDEN, "icosahedral_rotations.npz"))["R"]
     G = CvoGPU.rotation_grid(0).astype(np.float64)
-    assert len(ref) == 60
+    assert ref.shape == (60, 3, 3)
     for R in ref:
         assert np.min(np.abs(G - R).reshape(60, -1).max(1)) < 2e-6
+    for R in G:
+        assert np.min(np.abs(ref - R).reshape(60, -1).max(1)) < 2e-6
 
 
 def test_demo_pcd_fixture_reads_like_reference():
@@ -401,9 +402,59 @@ def test_golden_oracle_outputs_stable():
     g = np.load(os.path.join(GOLDEN, "demo_oracle.npz"))
     src = CvoPointCloud(d["src_xyz"], d["src_feat"])
     tgt = CvoPointCloud(d["tgt_xyz"], d["tgt_feat"])
-    p = CvoParams(params_path("color"))
+    p = OracleParams(params_path("color"))
     p.MAX_ITER = int(g["max_iter"])
     v, z = orc.inner_product_gpu_semantics(p, src, tgt, np.eye(4), float(g["ell"]))
     assert z == int(g["ip_nnz"]) and v == pytest.approx(float(g["ip"]), rel=1e-12)
     ret, T, iters, _ = orc.align(p, src, tgt, np.eye(4))
     assert iters == int(g["iters"]) and np.allclose(T, g["T_out"], atol=1e-6)
+
+
+# ------------------------------------------------------------------ parameters
+def _same_params(a, b):
+    da, db = a.as_dict(), b.as_dict()
+    assert da.keys() == db.keys()
+    for k in da:
+        assert np.float32(da[k]) == np.float32(db[k]) if isinstance(da[k], float) else da[k] == db[k], k
+
+
+def test_oracle_params_layout_matches_library():
+    """The oracle's parameter structure has the library's layout (both follow
+    struct cvo_params of include/cvo_gb300.h, which the C oracle reads)."""
+    import ctypes as C
+    from rkhs_ba_gb300 import _lib as L
+    assert C.sizeof(ParamsC) == C.sizeof(L.CvoParamsC)
+    for (fa, ta), (fb, tb) in zip(ParamsC._fields_, L.CvoParamsC._fields_):
+        assert fa == fb and ta == tb and getattr(ParamsC, fa).offset == getattr(L.CvoParamsC, fb).offset
+
+
+@pytest.mark.parametrize("name", ["geometric", "color", "lidar_semantic", "irls", None])
+def test_oracle_yaml_reader_agrees_with_library(name):
+    """Two independent readers of the parameter files -- the oracle's (Python) and
+    the library's (C++, cvo_params_read_yaml) -- give the same values, so the
+    parity tests do not rest on one parser (None: the constructor defaults)."""
+    path = params_path(name) if name else None
+    _same_params(OracleParams(path), CvoParams(path))
+
+
+def test_oracle_yaml_reader_edge_cases(tmp_path):
+    """Comments, quotes, repeated and unknown keys, keys the reference never reads
+    from a file, and values yaml-cpp would reject: both readers agree."""
+    from rkhs_ba_gb300._lib import CvoError
+    f = tmp_path / "p.yaml"
+    f.write_text("%YAML:1.0\n---\n# comment line\nsigma: 0.25   # trailing comment\n"
+                 "c_ell: '0.05'\nMAX_ITER: 40\nMAX_ITER: 41\nnot_a_field: 3\nstep: 9.0\n"
+                 "multiframe_iter_per_ell: 77\nmultiframe_iterations_per_ell: 12\ndl: 1e-3\n"
+                 "is_using_intensity: +1\n...\n")
+    o, p = OracleParams(str(f)), CvoParams(str(f))
+    _same_params(o, p)
+    assert o.MAX_ITER == 41 and o.step == 0.0 and o.multiframe_iter_per_ell == 10
+    assert o.multiframe_iterations_per_ell == 12 and o.is_using_intensity == 1
+    assert np.float32(o.c_ell) == np.float32(0.05) and o.dl == 1e-3
+    assert read_yaml_dict(str(f))["sigma"] == 0.25
+    bad = tmp_path / "bad.yaml"
+    bad.write_text("MAX_ITER: 1.5\n")
+    with pytest.raises(ValueError):
+        OracleParams(str(bad))
+    with pytest.raises(CvoError):
+        CvoParams(str(bad))
