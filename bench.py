@@ -40,16 +40,12 @@ METRIC = "registrations/s @50k pts: batched+learned vs plain grid, equal accurac
 UNIT = "registrations/s"
 
 
-def _profile_value(name, key):
-    """A `key: value` line of a committed profile summary (profiles/<name>), or None."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    with open(path) as fh:
-        for line in fh:
-            if line.startswith(key + ":"):
-                return float(line.split(":", 1)[1])
-    return None
+def _capture_value(key):
+    """A per-pair figure of the committed association capture
+    (profiles/k_assoc_cta_global50k.json, written by rkhs_ba_gb300.profiling), or None."""
+    from rkhs_ba_gb300 import profiling
+    d = profiling.load("k_assoc_cta_global50k.json")
+    return None if d is None else d.get(key)
 
 
 def issue_roofline(inst_per_pair, pair_passes, launches, avg_launch_s, sms, sm_mhz):
@@ -66,8 +62,8 @@ def issue_roofline(inst_per_pair, pair_passes, launches, avg_launch_s, sms, sm_m
     peak = sms * 4 * sm_mhz * 1e6 / 1e9
     return {"achieved": round(achieved, 2), "peak": round(peak, 2), "unit": "G warp instructions/s",
             "frac": round(achieved / peak, 4), "warp_instructions_per_launch": round(inst),
-            "note": "k_assoc_cta instructions from profiles/k_assoc_cta_global50k.md over the whole association "
-                    "phase's duration; peak = SMs x 4 schedulers x SM clock"}
+            "note": "k_assoc_cta instructions per pair from the committed ncu capture summary over the whole "
+                    "association phase's duration; peak = SMs x 4 schedulers x SM clock"}
 
 
 def _peaks():
@@ -176,6 +172,17 @@ def _proposal(args, cvo):
     if args.save_proposal:
         net.save(args.save_proposal)
     return net, info
+
+
+def workload_config(args):
+    """The `config` of both arms' JSON lines (the same workload)."""
+    return {"workload": "global registration, learned proposal (8 hypotheses, best %d refined) + CVO refinement, "
+                        "24-rotation grid fallback" % args.refine,
+            "points_per_cloud": args.points, "pairs_per_step": args.pairs, "params": "color.yaml",
+            "rotation": "uniform SO(3)", "translation_max_m": 2.0, "fallback_cos": args.fallback_cos,
+            "refine_ell": args.refine_ell,
+            "l2": "256 MB buffer written between timed steps",
+            "parallelism": "replicas"}
 
 
 def _success(Ts, pairs):
@@ -353,6 +360,27 @@ def run_ours(args):
             c.free()
     e2e_value, _ = replica_rate(args.pairs, float(np.mean(e2e_ms)), dist, "cuda")
 
+    # ---- like-for-like units the reference arm also reports, on the same pairs
+    H0 = net.hypotheses([gs[0]], [gt[0]])[0]
+    cos_ms = []
+    for k in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        cvo.inner_product_batch(gs[0], gt[0], list(H0), p.ell_init_first_frame)
+        e1.record(stream)
+        e1.synchronize()
+        cos_ms.append(e0.elapsed_time(e1))
+    pair_iters = sum(int(i) for r in results for i in r[1])
+    like = {"cos_angles_per_s": round(len(H0) / (float(np.median(cos_ms)) / 1000.0), 2),
+            "cos_angles_note": "the 8 hypotheses of the first pair in one batched call (GPU cap semantics)",
+            "align_iterations_per_s": round(pair_iters / (float(np.sum(step_ms)) / 1000.0), 2),
+            "align_iterations_note": "pair iterations of the timed learned steps over their whole duration "
+                                     "(ranking and judging included, so a lower bound on the align rate)"}
+    weights_match = None
+    if os.path.exists(WEIGHTS) and not args.proposal_weights:
+        weights_match = bool(np.array_equal(np.load(WEIGHTS).astype(np.float32), net.weights().astype(np.float32)))
+
     # ---- roofline of the association kernel
     peak, peak_kind = _peaks()
     roof = None
@@ -360,12 +388,12 @@ def run_ours(args):
         per_launch_bytes = prof["assoc_bytes"] / prof["assoc_launches"]
         avg_s = prof["assoc_ms"] / prof["assoc_launches"] / 1000.0
         achieved = per_launch_bytes / avg_s / 1e9
-        # DRAM bytes of one association launch: the ncu capture's bytes per pair
-        # (profiles/k_assoc_cta_global50k.md) times the mean number of pairs a launch
-        # of this run served (pair iterations / launches)
+        # DRAM bytes of one association launch: the committed ncu capture's bytes per
+        # pair times the mean number of pairs a launch of this run served (pair
+        # iterations / launches)
         traffic = None
         pair_passes = sum(int(i) for r in results for i in r[1])
-        per_pair = _profile_value("k_assoc_cta_global50k.md", "dram_bytes_per_pair_launch")
+        per_pair = _capture_value("dram_bytes_per_pair_launch")
         if per_pair is not None and pair_passes > 0:
             traffic = round(per_pair * pair_passes / prof["assoc_launches"])
         roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -377,7 +405,7 @@ def run_ours(args):
             sms = torch.cuda.get_device_properties(local).multi_processor_count
         except Exception:
             sms = None
-        roof["issue"] = issue_roofline(_profile_value("k_assoc_cta_global50k.md", "warp_instructions_per_pair_launch"),
+        roof["issue"] = issue_roofline(_capture_value("warp_instructions_per_pair_launch"),
                                        pair_passes, prof["assoc_launches"], avg_s, sms,
                                        clk.get("sm_mhz") or clk.get("sm_max_mhz"))
 
@@ -386,19 +414,15 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16 operands, f32 accumulation)",
         "data": "synthetic (seeded scenes)",
-        "config": {"workload": "global registration, learned proposal (8 hypotheses, best %d refined) + batched CVO, "
-                               "24-rotation grid fallback" % args.refine,
-                   "points_per_cloud": args.points, "pairs_per_step": args.pairs, "params": "color.yaml",
-                   "rotation": "uniform SO(3)", "translation_max_m": 2.0, "fallback_cos": args.fallback_cos,
-                   "refine_ell": args.refine_ell,
-                   "l2": "256 MB buffer written between timed steps", "parallelism": "replicas"},
+        "config": workload_config(args),
         "accuracy": {"success_rate": float(np.mean(succ)), "criterion": "rot<2deg, trans<5cm",
                      "mean_iters": float(np.mean(its)), "fallbacks": int(np.sum(fb))},
         "plain_grid": {"value": round(grid_value, 4), "unit": UNIT, "success_rate": float(np.mean(grid_succ)),
                        "mean_iters": float(np.mean(grid_res[-1][1])), "steps": len(grid_ms),
                        "note": "nearest of the 24 grid rotations by cos-angle, then one batched align"},
         "plain_grid_all24": all24,
-        "proposal": prop_info,
+        "proposal": dict(prop_info, weights_equal_committed=weights_match),
+        "like_for_like": like,
         "autotune": tune,
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -408,44 +432,97 @@ def run_ours(args):
         "wall_s": round(wall, 3),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, pairs[0], float(np.mean(grid_res[-1][1])))
+        out["cpu_baseline"] = cpu_baseline(args, pairs[0], net.weights())
     if rank == 0:
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
 
 
-def cpu_baseline(args, pair, iters_per_reg, budget_s=None):
-    """The CPU oracle on a bounded sample of the workload: the 24-rotation grid with the
-    reference's CPU inner product (radius search, all host threads) on one pair, plus a
-    few iterations of the CPU align loop; scaled to one registration using the GPU
-    run's mean iteration count."""
-    from oracle import oracle as orc
-    from rkhs_ba_gb300 import CvoGPU, CvoParams, params_path
+WEIGHTS = os.path.join(ROOT, "rkhs_ba_gb300", "weights", "proposal_color50k.npy")
 
-    p = CvoParams(params_path("color"))
-    src, tgt, _ = pair
-    cores = os.cpu_count() or 1
-    orc.set_threads(cores)
-    grid = CvoGPU.rotation_grid(1)
-    n_rot = len(grid) if args.cpu_rotations <= 0 else min(args.cpu_rotations, len(grid))
+
+class CpuLearned:
+    """The learned global registration of the timed workload, run on the host cores
+    with the oracle (the CPU restatement of the reference's path): the proposal
+    network's forward pass (oracle/proposal.py, numpy), the ranking of its 8
+    hypotheses by the approximate cos-angle with the reference's CPU inner product
+    (inner_product_cpu semantics: radius search, no cap, CvoGPU.cpp:113-231), the
+    refinement of the best one by the oracle's align loop (align_impl,
+    CvoGPU.cu:1239-1477) from --refine-ell, and the final cos-angle that judges it.
+    Loads nothing from the product library: parameters come from the oracle's own
+    yaml reader and the network weights from the committed file WEIGHTS (the
+    deterministic output of the device training the GPU arm runs)."""
+
+    def __init__(self, args, weights=None):
+        from oracle import oracle as orc
+        from oracle import proposal as op
+        from oracle.params import OracleParams
+        from rkhs_ba_gb300 import params_path
+        self.orc, self.op = orc, op
+        self.p = OracleParams(params_path("color"))
+        self.refine_ell = args.refine_ell if args.refine_ell > 0 else self.p.ell_init
+        if weights is None:
+            weights = np.load(args.proposal_weights or WEIGHTS)
+        self.w = np.asarray(weights, np.float32)
+        self.cores = os.cpu_count() or 1
+        orc.set_threads(self.cores)
+
+    def hypotheses(self, src, tgt, seed=0, P=512):
+        op = self.op
+        I = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32)
+        X = np.zeros((2, P, op.IN), np.float32)
+        cent = np.zeros((2, 3), np.float32)
+        for side, c in ((0, src), (1, tgt)):
+            _, cent[side], X[side] = op.slot_input(c.xyz, c.features, I, seed, side, P)
+        act = op.forward(self.w, X, 1, bf16_ops=True)
+        return op.hypotheses(act["O"], cent)[0].astype(np.float32)
+
+    def cos(self, src, tgt, T, ell):
+        ip, _ = self.orc.inner_product_cpu_semantics(self.p, src, tgt, T, ell)
+        return ip / np.sqrt(float(src.num_points()) * float(tgt.num_points()))
+
+    def register(self, pair, max_iter=None):
+        """One registration (max_iter limits the refinement: a bounded sample).  Returns
+        (pose, iterations, {phase: seconds})."""
+        src, tgt, _ = pair
+        t = {}
+        t0 = time.perf_counter()
+        H = self.hypotheses(src, tgt)
+        t["network"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        cosv = [self.cos(src, tgt, H[k], self.p.ell_init_first_frame) for k in range(len(H))]
+        t["rank"] = time.perf_counter() - t0
+        q = self.p.copy()
+        q.ell_init = self.refine_ell
+        if max_iter is not None:
+            q.MAX_ITER = max_iter
+        t0 = time.perf_counter()
+        ret, T, iters, _ = self.orc.align(q, src, tgt, H[int(np.argmax(cosv))])
+        t["refine"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        self.cos(src, tgt, np.linalg.inv(T.astype(np.float64)).astype(np.float32), self.p.ell_init_first_frame)
+        t["judge"] = time.perf_counter() - t0
+        return T, int(iters), t
+
+
+def cpu_baseline(args, pair, weights=None):
+    """One complete registration of one pair of the workload by the same pipeline on the
+    host cores (CpuLearned, with the network weights the GPU arm trained), timed end to
+    end: about half a minute of CPU work on a 16-core host."""
+    cl = CpuLearned(args, weights)
     t0 = time.perf_counter()
-    for r in range(n_rot):
-        T = np.eye(4, dtype=np.float32)
-        T[:3, :3] = grid[r].T
-        orc.function_angle(p, src, tgt, T, p.ell_init_first_frame, True, False)
-    t_grid = (time.perf_counter() - t0) * len(grid) / n_rot
-    q = p.copy()
-    q.MAX_ITER = args.cpu_iters
-    t0 = time.perf_counter()
-    orc.align(q, src, tgt, np.eye(4))
-    t_iter = (time.perf_counter() - t0) / args.cpu_iters
-    per_reg = t_grid + t_iter * iters_per_reg
-    return {"value": round(1.0 / per_reg, 6), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of 24 grid cos-angles (reference CPU inner-product semantics) + %d align iterations "
-                      "on one %d-point pair; scaled to 24 rotations + %.0f iterations per registration"
-                      % (n_rot, args.cpu_iters, src.num_points(), iters_per_reg),
-            "seconds_per_registration": round(per_reg, 3)}
+    _, iters, t = cl.register(pair)
+    sec = time.perf_counter() - t0
+    src = pair[0]
+    return {"value": round(1.0 / sec, 6), "unit": UNIT, "cores": cl.cores, "kind": "port",
+            "sample": "one complete registration of the first %d-point pair of the workload by the same pipeline "
+                      "(network forward, 8 CPU cos-angles, CPU align from ell %.2f: %d iterations, CPU judge)"
+                      % (src.num_points(), cl.refine_ell, iters),
+            "seconds_per_registration": round(sec, 3), "iterations": iters,
+            "phase_s": {k: round(v, 3) for k, v in t.items()},
+            "cos_angles_per_s": round(9.0 / (t["rank"] + t["judge"]), 4),
+            "align_iterations_per_s": round(iters / t["refine"], 4)}
 
 
 def run_component(args):
@@ -732,27 +809,53 @@ def run_component(args):
 
 
 def run_reference(args):
+    """The reference arm: the workload's learned global registration on the host cores
+    (CpuLearned), on the GPU arm's config, metric and unit.
+
+    value: registrations/s of --ref-full-pairs complete registrations of the workload's
+    first pairs, each timed end to end (network, ranking, refinement to convergence,
+    judge).  The --warmup and --steps steps are bounded samples of the 8-pair step: pair
+    (step mod 8) goes through the whole pipeline with its refinement limited to
+    --ref-sample-iters iterations; ms_per_step is their measured wall time, and the
+    cos-angles/s and align iterations/s they measure are the like-for-like units the GPU
+    arm also reports."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pairs = make_pairs(1, args.points)
-    samples = []
     t_all = time.perf_counter()
-    cb = None
-    for _ in range(max(0, args.warmup)):
-        cpu_baseline(args, pairs[0], args.ref_iters)
-    for _ in range(max(1, args.steps)):
-        cb = cpu_baseline(args, pairs[0], args.ref_iters)
-        samples.append(1.0 / cb["seconds_per_registration"])
-    value = float(np.mean(samples))
+    pairs = make_pairs(args.pairs, args.points, seed0=1000)
+    cl = CpuLearned(args)
+    full = []
+    for k in range(max(1, min(args.ref_full_pairs, len(pairs)))):
+        t0 = time.perf_counter()
+        _, it, ph = cl.register(pairs[k])
+        full.append({"pair": k, "seconds": round(time.perf_counter() - t0, 3), "iterations": it,
+                     "phase_s": {n: round(v, 3) for n, v in ph.items()}})
+    value = len(full) / sum(f["seconds"] for f in full)
+    S = max(1, args.ref_sample_iters)
+    for k in range(max(0, args.warmup)):
+        cl.register(pairs[k % len(pairs)], max_iter=S)
+    cos_s, iter_s, iters, step_s = 0.0, 0.0, 0, []
+    for k in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        _, it, t = cl.register(pairs[k % len(pairs)], max_iter=S)
+        step_s.append(time.perf_counter() - t0)
+        cos_s += t["rank"] + t["judge"]
+        iter_s += t["refine"]
+        iters += it
     out = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "impl": "reference", "n_gpus": 1,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / value, 3), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-           "config": {"workload": "global registration, plain 24-rotation grid + CVO refine (CPU)",
-                      "points_per_cloud": args.points, "pairs_per_step": 1, "params": "color.yaml",
-                      "note": "reference CPU path restated (the reference cannot be compiled here)"},
-           "cpu_baseline": {"kind": "port", "cores": cb["cores"], "sample": cb["sample"], "value": round(value, 6),
-                            "unit": UNIT},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * float(np.mean(step_s)), 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded scenes)", "config": workload_config(args),
+           "full_registrations": full,
+           "measured": {"cos_angles_per_s": round(9 * len(step_s) / cos_s, 4),
+                        "align_iterations_per_s": round(iters / iter_s, 4),
+                        "note": "from the timed sample steps: 9 CPU cos-angles and %d align iterations (from ell "
+                                "%.2f, the most expensive part of a refinement) per step" % (S, cl.refine_ell)},
+           "cpu_baseline": {"kind": "port", "cores": cl.cores, "value": round(value, 6), "unit": UNIT,
+                            "sample": "%d complete registrations of the workload's first pairs on all host threads "
+                                      "(value); per step one of the 8 pairs through network, ranking, %d align "
+                                      "iterations and judge (ms_per_step)" % (len(full), S)},
            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "wall_s": round(time.perf_counter() - t_all, 3)}
     print(json.dumps(out))
@@ -766,11 +869,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=8)
     ap.add_argument("--points", type=int, default=50000)
-    ap.add_argument("--cpu-iters", type=int, default=2)
-    ap.add_argument("--cpu-rotations", type=int, default=4)
-    # iterations per registration the reference arm scales its sample to: the mean the
-    # same algorithm takes on this workload (251 on the 8 seeded pairs)
-    ap.add_argument("--ref-iters", type=float, default=251.0)
+    ap.add_argument("--cpu-iters", type=int, default=2, help="oracle iterations timed by --component adaptive")
+    ap.add_argument("--ref-sample-iters", type=int, default=2,
+                    help="align iterations of the refinement in each step of the reference arm's sample")
+    ap.add_argument("--ref-full-pairs", type=int, default=2,
+                    help="complete CPU registrations the reference arm's value is measured on")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refine", type=int, default=1, help="hypotheses refined per pair (1..8)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default association cell size")

@@ -11,22 +11,36 @@ import os
 import subprocess
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "0", "--points", "2000", "--cpu-rotations", "1",
-        "--cpu-iters", "1"]
+ARGS = ["--impl", "reference", "--steps", "2", "--warmup", "1", "--points", "2000", "--pairs", "2",
+        "--ref-sample-iters", "1"]
 
 
-def _run(env_extra=None):
+def _weights(tmp_path):
+    """Network weights of the right size for the CPU pipeline (random: the contract only)."""
+    sys.path.insert(0, ROOT)
+    from oracle import proposal as op
+    path = str(tmp_path / "w.npy")
+    np.save(path, (np.random.default_rng(0).normal(size=op.NUM_PARAMS) * 0.05).astype(np.float32))
+    return path
+
+
+def _run(tmp_path, env_extra=None):
     env = dict(os.environ)
     env.update(env_extra or {})
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *ARGS], cwd=ROOT, env=env,
-                       capture_output=True, text=True, timeout=300)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *ARGS, "--proposal-weights", _weights(tmp_path)],
+                       cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     return [l for l in r.stdout.splitlines() if l.strip()]
 
 
-def test_reference_arm_prints_one_contract_line():
-    lines = _run()
+def test_reference_arm_prints_one_contract_line(tmp_path):
+    """The reference arm: the workload's pipeline on the host cores through the oracle,
+    with the GPU arm's config; ms_per_step is the measured wall time of a step, the value
+    is derived from measured per-phase times, and the product library is never loaded."""
+    lines = _run(tmp_path)
     assert len(lines) == 1
     d = json.loads(lines[0])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
@@ -34,7 +48,13 @@ def test_reference_arm_prints_one_contract_line():
         assert k in d, k
     assert d["impl"] == "reference"
     assert d["unit"] == "registrations/s" and d["higher_is_better"] is True
-    assert d["value"] > 0 and abs(d["ms_per_step"] - 1000.0 / d["value"]) <= 1e-3 * d["ms_per_step"] + 1e-3
+    assert d["value"] > 0 and d["ms_per_step"] > 0 and d["steps"] == 2 and d["warmup"] == 1
+    full = d["full_registrations"]
+    assert len(full) == 2 and all(f["iterations"] >= 1 and f["seconds"] > 0 for f in full)
+    assert abs(d["value"] - 2 / sum(f["seconds"] for f in full)) <= 1e-3 * d["value"]
+    m = d["measured"]
+    assert m["cos_angles_per_s"] > 0 and m["align_iterations_per_s"] > 0
+    assert d["config"]["pairs_per_step"] == 2 and d["config"]["points_per_cloud"] == 2000
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     cb = d["cpu_baseline"]
@@ -42,8 +62,24 @@ def test_reference_arm_prints_one_contract_line():
     assert "workload" in d["config"]
 
 
-def test_reference_arm_other_ranks_are_silent():
-    assert _run({"RANK": "1", "WORLD_SIZE": "2"}) == []
+def test_reference_arm_other_ranks_are_silent(tmp_path):
+    assert _run(tmp_path, {"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_reference_arm_loads_no_product_library(tmp_path):
+    """The CPU pipeline of the reference arm maps the oracle's library, never the
+    product's (parameters from the oracle's yaml reader, weights from a file)."""
+    code = ("import sys, json, argparse; sys.path.insert(0, %r); import bench;"
+            "a = argparse.Namespace(refine_ell=0.4, proposal_weights=%r);"
+            "cl = bench.CpuLearned(a); from rkhs_ba_gb300 import scenes;"
+            "pair = scenes.global_pair(1500, 7); T, it, t = cl.register(pair, max_iter=2);"
+            "maps = open('/proc/self/maps').read();"
+            "print(json.dumps({'product': 'libcvo_gb300' in maps, 'oracle': 'libcvo_oracle' in maps, 'it': it}))"
+            % (ROOT, _weights(tmp_path)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["oracle"] and not d["product"] and 1 <= d["it"] <= 2
 
 
 def test_issue_roofline_arithmetic():
@@ -58,7 +94,7 @@ def test_issue_roofline_arithmetic():
     assert bench.issue_roofline(None, 2, 1, 1e-3, 152, 2000.0) is None
     assert bench.issue_roofline(1e6, 0, 1, 1e-3, 152, 2000.0) is None
     assert bench.issue_roofline(1e6, 2, 1, 1e-3, None, 2000.0) is None
-    v = bench._profile_value("k_assoc_cta_global50k.md", "warp_instructions_per_pair_launch")
+    v = bench._capture_value("warp_instructions_per_pair_launch")
     assert v is not None and v > 1e8
 
 
@@ -117,6 +153,9 @@ def main():
         def hypotheses(self, gs, gt):
             return np.tile(np.eye(4, dtype=np.float32), (len(gs), 8, 1, 1))
 
+        def weights(self):
+            return np.zeros(self.num_params, np.float32)
+
     class FakeCvo:
         rotation_grid = staticmethod(rkhs_ba_gb300.CvoGPU.rotation_grid)
 
@@ -140,6 +179,9 @@ def main():
         def align_batch(self, gs, gt, inits):
             k = len(gs)
             return np.tile(np.eye(4), (k, 1, 1)), np.zeros(k, np.int32), np.full(k, 250), 0.1
+
+        def inner_product_batch(self, s, t, Ts, ell):
+            return np.ones(len(Ts), np.float32)
 
         def register_hypotheses(self, s, t, Ts, ell):
             return np.eye(4), 0, np.ones(len(Ts)), 0.1
@@ -174,8 +216,8 @@ def main():
     rkhs_ba_gb300.CvoGPU = FakeCvo
     bench._proposal = lambda args, cvo: (FakeNet(), {"fake": True})
     bench.ClockSampler = FakeClocks
-    sys.argv = ["bench.py"] + (sys.argv[2:] or ["--pairs", "2", "--points", "2000", "--steps", "3", "--warmup", "3",
-                                                "--all24-pairs", "1", "--cpu-rotations", "1", "--cpu-iters", "1"])
+    sys.argv = ["bench.py"] + (sys.argv[3:] or ["--pairs", "2", "--points", "2000", "--steps", "3", "--warmup", "3",
+                                                "--all24-pairs", "1"]) + ["--proposal-weights", sys.argv[2]]
     bench.main()
 
 
@@ -192,7 +234,8 @@ def test_ours_arm_json_with_a_faked_gpu(tmp_path):
     the kernels are covered by the gpu-marked tests."""
     script = tmp_path / "fake_gpu_bench.py"
     script.write_text(_FAKE_GPU_CHILD)
-    r = subprocess.run([sys.executable, str(script), ROOT], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, str(script), ROOT, _weights(tmp_path)], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
     d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
@@ -211,7 +254,7 @@ def test_global_eval_component_with_a_faked_gpu(tmp_path):
     its own Python end to end with the GPU faked: batches, success rates, JSON."""
     script = tmp_path / "fake_gpu_bench.py"
     script.write_text(_FAKE_GPU_CHILD)
-    r = subprocess.run([sys.executable, str(script), ROOT, "--component", "global-eval", "--eval-pairs", "5",
+    r = subprocess.run([sys.executable, str(script), ROOT, _weights(tmp_path), "--component", "global-eval", "--eval-pairs", "5",
                         "--pairs", "2", "--points", "2000"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
     d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
@@ -227,7 +270,7 @@ def test_batching_component_with_a_faked_gpu(tmp_path):
     registration, for uneven pairs and for the 24 grid hypotheses) with the GPU faked."""
     script = tmp_path / "fake_gpu_bench.py"
     script.write_text(_FAKE_GPU_CHILD)
-    r = subprocess.run([sys.executable, str(script), ROOT, "--component", "batching", "--pairs", "2", "--points", "2000",
+    r = subprocess.run([sys.executable, str(script), ROOT, _weights(tmp_path), "--component", "batching", "--pairs", "2", "--points", "2000",
                         "--steps", "1", "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
     d = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])

@@ -183,3 +183,23 @@ def test_invalid_arguments_are_rejected(cvo, small_pool):
     # hypotheses of an empty cloud are defined (identity rotation block, centroid 0) and finite
     H = net.hypotheses([gs], [empty])
     assert H.shape == (1, 8, 4, 4) and np.all(np.isfinite(H))
+
+
+def test_cpu_pipeline_hypotheses_equal_device(cvo):
+    """The bench's reference arm computes the network's hypotheses on the host
+    (bench.CpuLearned: oracle forward with the committed weights); they are the
+    device's hypotheses for the same device-resident pair and weights."""
+    import argparse
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    cl = bench.CpuLearned(argparse.Namespace(refine_ell=0.4, proposal_weights=""))
+    net = ProposalNet(cvo, points_per_cloud=512, seed=0)
+    net.set_weights(cl.w)
+    src, tgt, _ = scenes.global_pair(n=20000, seed=1234)
+    H_dev = net.hypotheses([cvo.upload(src)], [cvo.upload(tgt)])[0]
+    H_cpu = cl.hypotheses(src, tgt)
+    assert np.allclose(H_dev[:, :3, :3], H_cpu[:, :3, :3], atol=1e-4)
+    assert np.allclose(H_dev[:, :3, 3], H_cpu[:, :3, 3], atol=1e-3 * (1 + np.abs(H_cpu[:, :3, 3]).max()))
