@@ -7,9 +7,10 @@
 // streams their members through shared memory 128 candidates at a time: every
 // thread loads one candidate (coalesced) and builds its prefilter vector, and each
 // warp runs the tensor-core prefilter of its 32 rows against all 128 candidates and
-// the exact per-pair evaluation of the survivors.  Candidate order (cell list
-// order, members ascending) is fixed, so rows receive their kept pairs in a
-// deterministic order.  Blocks whose union box is sparse, or whose prefilter
+// the exact per-pair evaluation of the survivors.  A row's first `cap` kept pairs
+// go to its ELL slots and any further ones to its spill list (put_kept).  Candidate
+// order (cell list order, members ascending) is fixed, so rows receive their kept
+// pairs in a deterministic order.  Blocks whose union box is sparse, or whose prefilter
 // vectors leave the f16 range, run the per-warp path instead.
 #pragma once
 #include "cvo_kernels.cuh"
@@ -196,14 +197,7 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
   int cnt = 0;
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;
-  auto put = [&](int r, int slot, int j, float a) {
-    const size_t sidx = (size_t)(tile0 + r);
-    if (slot < cap) {
-      P->A_j[(size_t)slot * n + sidx] = j;
-      P->A_v[(size_t)slot * n + sidx] = a;
-    }
-    if (slot < ov) P->ovf[sidx * ov + slot] = make_int2(j, __float_as_int(a));
-  };
+  auto put = [&](int r, int slot, int j, float a) { put_kept(P, n, cap, ov, (size_t)(tile0 + r), slot, j, a); };
   // cells farther than the largest radius from every query point are skipped
   const float slack = 1e-3f * G.h;
   const float prune_r2 = (brq + slack) * (brq + slack);

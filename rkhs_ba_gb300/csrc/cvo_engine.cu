@@ -235,10 +235,9 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
     float coef = __double2float_rn(__ddiv_rn(1.0, dm(dm(2.0, (double)tl), (double)tl)));
     const int z = P->nnz_row[s];
     const float4 *__restrict__ yorig = P->yorig;
-    for (int c = 0; c < z; c++) {
-      int j = P->A_j[(size_t)c * n + s];
-      float a = P->A_v[(size_t)c * n + s];
-      float4 y = __ldg(&yorig[j]);
+    const int *__restrict__ Aj = P->A_j + s;
+    const float *__restrict__ Av = P->A_v + s;
+    auto add = [&](float a, const float4 &y) {
       float ux = w1 * y.z - w2 * y.y + u0v, uy = w2 * y.x - w0 * y.z + u1v, uz = w0 * y.y - w1 * y.x + u2v;
       float px = w1 * uz - w2 * uy, py = w2 * ux - w0 * uz, pz = w0 * uy - w1 * ux;          // xi^2 z
       float qx = w1 * pz - w2 * py, qy = w2 * px - w0 * pz, qz = w0 * py - w1 * px;          // xi^3 z
@@ -256,7 +255,21 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
       Cs += a * (gamma + 0.5f * b2);
       Ds += a * (delta + beta * gamma + b2 * beta * (1.f / 6.f));
       Es += a * (epsil + beta * delta + 0.5f * b2 * gamma + 0.5f * gamma * gamma + b2 * b2 * (1.f / 24.f));
+    };
+    int c = 0;
+    // four entries' loads in flight at a time; the sums keep slot order
+    for (; c + 4 <= z; c += 4) {
+      const int j0 = Aj[(size_t)c * n], j1 = Aj[(size_t)(c + 1) * n], j2 = Aj[(size_t)(c + 2) * n],
+                j3 = Aj[(size_t)(c + 3) * n];
+      const float a0 = Av[(size_t)c * n], a1 = Av[(size_t)(c + 1) * n], a2 = Av[(size_t)(c + 2) * n],
+                  a3 = Av[(size_t)(c + 3) * n];
+      const float4 y0 = __ldg(&yorig[j0]), y1 = __ldg(&yorig[j1]), y2 = __ldg(&yorig[j2]), y3 = __ldg(&yorig[j3]);
+      add(a0, y0);
+      add(a1, y1);
+      add(a2, y2);
+      add(a3, y3);
     }
+    for (; c < z; c++) add(Av[(size_t)c * n], __ldg(&yorig[Aj[(size_t)c * n]]));
   }
   double v[4] = {Bs, Cs, Ds, Es};
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -545,7 +558,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
   int max_part_blocks = 0;
-  // row-list entries per row (every kept pair, row-major): up to kSelMax, at most 8 GB for the batch
+  // spill-list entries per row (kept pairs beyond cap, row-major): up to kSelMax, at most 8 GB for the batch
   long long rows_all = 0;
   for (int p = 0; p < np; p++) rows_all += srcs[p]->n;
   int ov = kSelMax;
@@ -565,7 +578,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     add(sizeof(float4) * m);                                     // yorig
     add(sizeof(int) * (size_t)n * capmax);                       // ELL (every mode: the row selection uses it)
     add(sizeof(float) * (size_t)n * capmax);
-    add(sizeof(int2) * (size_t)n * ov);                          // row lists
+    add(sizeof(int2) * (size_t)n * ov);                          // spill lists
     add(sizeof(int) * n);                                        // nnz_row
     add(sizeof(float) * 8 * (size_t)n);                          // row_sums
     add(sizeof(double) * kPartStride * (size_t)std::max(rb, sb)); // partials

@@ -4,7 +4,7 @@
 // fixed sequence of launches over every active pair of a batch:
 //   k_transform  target transform y' = R^T (y - T)            (CvoGPU_impl.cu:32-83)
 //   k_assoc_cta  association: grid candidates -> tensor-core prefilter -> exact kernel
-//                value -> threshold -> ELL row (first cap) + row list
+//                value -> threshold -> ELL row (first cap) + spill list (the rest)
 //                (cvo_assoc_cta.cuh; per-warp path assoc_warp below)
 //                                                               (CvoGPU.cu:951-1099)
 //   k_select / k_rescan  rows with more than cap kept pairs: their cap smallest indices
@@ -293,19 +293,40 @@ struct __align__(16) SrcRows {
   float g1[32];                                // geometric type g1
 };
 
-// Position of the (n+1)-th set bit of m (n >= 0, m has more than n set bits).
+// Position of the (n+1)-th set bit of m (n >= 0, m has more than n set bits):
+// a binary search on population counts of the low halves, fixed latency.
 __device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
-  for (int i = 0; i < n; i++) m &= m - 1u;
-  return __ffs(m) - 1;
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const uint32_t low = (m >> pos) & ((1u << w) - 1u);
+    const int c = __popc(low);
+    if (n >= c) {
+      n -= c;
+      pos += w;
+    }
+  }
+  return pos;
 }
 
 // Kept count of a finished row; a row with more than cap kept pairs is listed for
-// k_select (its row list holds them all) or k_rescan.
+// k_select (its ELL row and its spill list hold them all) or k_rescan.
 __device__ __forceinline__ void finish_row(const BatchDev &B, PairDev *P, int p, int s, int cnt, int cap, int ov) {
   P->nnz_row[s] = cnt < cap ? cnt : cap;
   if (cnt > cap && cap > 0) {
-    if (cnt <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
+    if (cnt - cap <= ov) B.sel_list[atomicAdd(B.sel_count, 1)] = make_int4(p, s, cnt, 0);
     else B.scan_list[atomicAdd(B.scan_count, 1)] = make_int4(p, s, cnt, 0);
+  }
+}
+
+// Stores kept pair number `slot` of source row sidx: the first cap go to the row's
+// ELL slots, the next ov to its spill list (row-major), the rest are only counted.
+__device__ __forceinline__ void put_kept(PairDev *P, int n, int cap, int ov, size_t sidx, int slot, int j, float a) {
+  if (slot < cap) {
+    P->A_j[(size_t)slot * n + sidx] = j;
+    P->A_v[(size_t)slot * n + sidx] = a;
+  } else if (slot - cap < ov) {
+    P->ovf[sidx * ov + (slot - cap)] = make_int2(j, __float_as_int(a));
   }
 }
 
@@ -586,15 +607,8 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
   const float4 *__restrict__ ycur = P->ycur;
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;   // source index of lane 0's row
-  // kept pair number `slot` of row r enters its ELL slot (first cap) and its row list
-  auto put = [&](int r, int slot, int j, float a) {
-    const size_t sidx = (size_t)(tile0 + r);
-    if (slot < cap) {
-      P->A_j[(size_t)slot * n + sidx] = j;
-      P->A_v[(size_t)slot * n + sidx] = a;
-    }
-    if (slot < ov) P->ovf[sidx * ov + slot] = make_int2(j, __float_as_int(a));
-  };
+  // kept pair number `slot` of row r enters its ELL slot (first cap) or its spill list
+  auto put = [&](int r, int slot, int j, float a) { put_kept(P, n, cap, ov, (size_t)(tile0 + r), slot, j, a); };
   for (int pass = 0; pass < npass; pass++) {
     int x0, y0, z0, nx, ny, nz;
     bool me = valid;
@@ -700,7 +714,7 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
 }
 
 // ------------------------------------------------------------ selection
-constexpr int kSelMax = 4096;      // kept pairs one row list can hold
+constexpr int kSelMax = 4096;      // kept pairs beyond cap one spill list can hold
 constexpr int kSelStage = 2048;    // rows up to this many entries are selected from shared memory
 constexpr int kSelThreads = 128;
 
@@ -717,9 +731,10 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
   const int z = P->nnz_row[s];
   const float4 x = __ldg(&P->xs[s]);
   float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
-  for (int c = 0; c < z; c++) {
-    const float a = P->A_v[(size_t)c * n + s];
-    const float4 y = __ldg(&P->yorig[P->A_j[(size_t)c * n + s]]);
+  const int *__restrict__ Aj = P->A_j + s;
+  const float *__restrict__ Av = P->A_v + s;
+  const float4 *__restrict__ yorig = P->yorig;
+  auto add = [&](float a, const float4 &y) {
     w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
     w1 = fmaf(a, fs(fm(x.z, y.x), fm(x.x, y.z)), w1);
     w2 = fmaf(a, fs(fm(x.x, y.y), fm(x.y, y.x)), w2);
@@ -727,20 +742,39 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
     v1 = fmaf(a, y.y - x.y, v1);
     v2 = fmaf(a, y.z - x.z, v2);
     as += a;
+  };
+  int c = 0;
+  // four entries' loads in flight at a time; the sums keep slot order
+  for (; c + 4 <= z; c += 4) {
+    const int j0 = Aj[(size_t)c * n], j1 = Aj[(size_t)(c + 1) * n], j2 = Aj[(size_t)(c + 2) * n],
+              j3 = Aj[(size_t)(c + 3) * n];
+    const float a0 = Av[(size_t)c * n], a1 = Av[(size_t)(c + 1) * n], a2 = Av[(size_t)(c + 2) * n],
+                a3 = Av[(size_t)(c + 3) * n];
+    const float4 y0 = __ldg(&yorig[j0]), y1 = __ldg(&yorig[j1]), y2 = __ldg(&yorig[j2]), y3 = __ldg(&yorig[j3]);
+    add(a0, y0);
+    add(a1, y1);
+    add(a2, y2);
+    add(a3, y3);
   }
+  for (; c < z; c++) add(Av[(size_t)c * n], __ldg(&yorig[Aj[(size_t)c * n]]));
   write_row_sums(P->row_sums + (size_t)s * 8, P->mode, K, w0, w1, w2, v0, v1, v2, as);
 }
 
-// One warp per listed row with cap < count <= ov: the row list (row-major, kept
-// pairs in the order they were kept) holds every kept pair of the row.  A radix
-// select over the bits of the target index (8-bit digits from the highest bit
-// the pair's target count needs, warp-private histograms in shared memory) finds
-// the cap-th smallest index r; the entries with index <= r (exactly cap, indices
-// are distinct) are written to the ELL slots in list order.  Indices are staged
-// in shared memory when the row fits (kSelStage entries).
+// One warp per listed row with cap < count <= cap + ov: its ELL slots hold the
+// first cap kept pairs and its spill list (row-major) the rest, in the order they
+// were kept.  A radix select over d = j - jmin (jmin, jmax: the row's smallest and
+// largest kept index; 9-bit digits from the highest bit of jmax - jmin, warp-private
+// histograms in shared memory) finds the cap-th smallest index r.  Offsetting by jmin
+// spreads neighbouring indices over the bins, so the histogram atomics rarely collide
+// and a row whose indices span fewer than 512 values needs one pass.  The entries
+// with index <= r (exactly cap: indices are distinct) are compacted in list order
+// into the ELL slots, in place (an entry is read before any write can reach its slot).
+// Indices are staged in shared memory when the row fits (kSelStage entries).
+constexpr int kSelBins = 512;
+constexpr int kSelDigit = 9;
 __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
-  __shared__ int hist_all[kSelThreads / 32][256];
+  __shared__ int hist_all[kSelThreads / 32][kSelBins];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *jb = jbuf_all[w];
   int *hist = hist_all[w];
@@ -752,60 +786,77 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     const int s = it.y, n = P->n, cap = P->cap, ov = P->ov;
     const int E = it.z;
     const int2 *lst = P->ovf + (size_t)s * ov;
+    int *Aj = P->A_j + s;
+    float *Av = P->A_v + s;
     const bool staged = E <= kSelStage;
-    if (staged) {
-      for (int t = lane; t < E; t += 32) jb[t] = lst[t].x;
+    auto gidx = [&](int t) -> int { return t < cap ? Aj[(size_t)t * n] : lst[t - cap].x; };
+    int jmin = 0x7FFFFFFF, jmax = -1;
+    for (int t = lane; t < E; t += 32) {
+      const int j = gidx(t);
+      if (staged) jb[t] = j;
+      jmin = min(jmin, j);
+      jmax = max(jmax, j);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      jmin = min(jmin, __shfl_xor_sync(FULLMASK, jmin, o));
+      jmax = max(jmax, __shfl_xor_sync(FULLMASK, jmax, o));
     }
     __syncwarp();
-    auto entry = [&](int t) -> int { return staged ? jb[t] : lst[t].x; };
-    const int bits = P->m > 1 ? 32 - __clz(P->m - 1) : 1;
+    auto entry = [&](int t) -> int { return staged ? jb[t] : gidx(t); };
+    const int span = jmax - jmin;
+    const int bits = span > 0 ? 32 - __clz(span) : 1;
     int prefix = 0, target = cap;
-    for (int hs = bits; hs > 0; hs -= 8) {
-      const int sh = max(hs - 8, 0), wd = hs - sh;
-      for (int b = lane; b < 256; b += 32) hist[b] = 0;
+    for (int hs = bits; hs > 0; hs -= kSelDigit) {
+      const int sh = max(hs - kSelDigit, 0), wd = hs - sh;
+      for (int b = lane; b < kSelBins; b += 32) hist[b] = 0;
       __syncwarp();
       for (int t = lane; t < E; t += 32) {
-        const int j = entry(t);
-        if ((j >> hs) == (prefix >> hs)) atomicAdd(&hist[(j >> sh) & ((1 << wd) - 1)], 1);
+        const int d = entry(t) - jmin;
+        if ((d >> hs) == (prefix >> hs)) atomicAdd(&hist[(d >> sh) & ((1 << wd) - 1)], 1);
       }
       __syncwarp();
+      constexpr int kPer = kSelBins / 32;
       int loc = 0;
 #pragma unroll
-      for (int i = 0; i < 8; i++) loc += hist[lane * 8 + i];
+      for (int i = 0; i < kPer; i++) loc += hist[lane * kPer + i];
       int incl = loc;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(FULLMASK, incl, o);
         if (lane >= o) incl += t;
       }
-      const int L = __ffs(__ballot_sync(FULLMASK, incl >= target)) - 1;
+      int L = __ffs(__ballot_sync(FULLMASK, incl >= target)) - 1;
+      if (L < 0) L = 31;             // unreachable: the counted entries always reach target
       int run = __shfl_sync(FULLMASK, incl - loc, L);
-      int bin = L * 8;
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const int hb = hist[L * 8 + i];
-        if (run + hb >= target) { bin = L * 8 + i; break; }
+      int bin = L * kPer;
+#pragma unroll 1
+      for (int i = 0; i < kPer; i++) {
+        const int hb = hist[L * kPer + i];
+        if (run + hb >= target) { bin = L * kPer + i; break; }
         run += hb;
       }
       prefix |= bin << sh;
       target -= run;
       __syncwarp();
     }
-    const int r = prefix;   // the cap-th smallest kept index
+    const int r = jmin + prefix;   // the cap-th smallest kept index
     int base = 0;
     for (int t0 = 0; t0 < E; t0 += 32) {
       const int t = t0 + lane;
-      int2 v = make_int2(0, 0);
+      int j = 0;
+      float a = 0.f;
       bool k = false;
       if (t < E) {
-        v = lst[t];
-        k = v.x <= r;
+        j = entry(t);
+        k = j <= r;
+        if (k) a = t < cap ? Av[(size_t)t * n] : __int_as_float(lst[t - cap].y);
       }
       const unsigned bal = __ballot_sync(FULLMASK, k);
-      if (k) {
-        const int c = base + __popc(bal & ((1u << lane) - 1u));
-        P->A_j[(size_t)c * n + s] = v.x;
-        P->A_v[(size_t)c * n + s] = __int_as_float(v.y);
+      const int c = base + __popc(bal & ((1u << lane) - 1u));
+      if (k && c < cap) {
+        Aj[(size_t)c * n] = j;
+        Av[(size_t)c * n] = a;
       }
       base += __popc(bal);
     }
@@ -813,7 +864,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   }
 }
 
-// One warp per listed row with count > ov: the reference's own order, i.e. a
+// One warp per listed row with count > cap + ov: the reference's own order, i.e. a
 // scan of the targets by ascending original index (32 per step, one per lane) that
 // stops once cap pairs are kept.  Same per-pair arithmetic as k_assoc.
 template <int FCH, int LCH, bool GT>
