@@ -62,11 +62,12 @@ __device__ __forceinline__ void block_sum_out(double (&v)[NV], double *out) {
     }
 }
 
-// ELL of one edge: entry c of (tile-order) row s at [c * n + s], original column indices.
+// ELL of one edge: entry c of (tile-order) row s at [s * ld + c], original column indices.
 struct Ell {
-  const int *j;
+  const int *j;       // row-major with pitch ld
   const float *v;
   const int *nnz;
+  int ld;
 };
 
 // Source rows (tile order xs): omega / c, v / d (FP32 per row, as
@@ -82,8 +83,8 @@ __global__ void __launch_bounds__(kAdRedThreads) k_ad_flow(int n, const float4 *
     float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, dl = 0.f;
     const int na = A.nnz[s];
     for (int t = 0; t < na; t++) {
-      const int j = A.j[(size_t)t * n + s];
-      const float a = A.v[(size_t)t * n + s];
+      const int j = A.j[(size_t)s * A.ld + t];
+      const float a = A.v[(size_t)s * A.ld + t];
       const float4 q = y[j];
       const float cx = fs(fm(p.y, q.z), fm(p.z, q.y)), cy = fs(fm(p.z, q.x), fm(p.x, q.z)), cz = fs(fm(p.x, q.y), fm(p.y, q.x));
       const float dx = fs(q.x, p.x), dy = fs(q.y, p.y), dz = fs(q.z, p.z);
@@ -95,8 +96,8 @@ __global__ void __launch_bounds__(kAdRedThreads) k_ad_flow(int n, const float4 *
     float dxx = 0.f;
     const int nx = X.nnz[s];
     for (int t = 0; t < nx; t++) {
-      const float4 q = xo[X.j[(size_t)t * n + s]];
-      dxx = fa(dxx, fm(sqdist3(q.x, q.y, q.z, p.x, p.y, p.z), X.v[(size_t)t * n + s]));
+      const float4 q = xo[X.j[(size_t)s * X.ld + t]];
+      dxx = fa(dxx, fm(sqdist3(q.x, q.y, q.z, p.x, p.y, p.z), X.v[(size_t)s * X.ld + t]));
     }
     v[0] = (double)__fdiv_rn(w0, c); v[1] = (double)__fdiv_rn(w1, c); v[2] = (double)__fdiv_rn(w2, c);
     v[3] = (double)__fdiv_rn(v0, d); v[4] = (double)__fdiv_rn(v1, d); v[5] = (double)__fdiv_rn(v2, d);
@@ -118,8 +119,8 @@ __global__ void __launch_bounds__(kAdRedThreads) k_ad_flow_yy(int m, const float
     float prod = 0.f;
     const int ny = Y.nnz[s];
     for (int t = 0; t < ny; t++) {
-      const float4 q = y[Y.j[(size_t)t * m + s]];
-      prod = fa(prod, fm(Y.v[(size_t)t * m + s], sqdist3(q.x, q.y, q.z, p.x, p.y, p.z)));
+      const float4 q = y[Y.j[(size_t)s * Y.ld + t]];
+      prod = fa(prod, fm(Y.v[(size_t)s * Y.ld + t], sqdist3(q.x, q.y, q.z, p.x, p.y, p.z)));
     }
     const float ell3 = fm(fm(ell, ell), ell);
     v[0] = (double)fm(__fdiv_rn(1.f, ell3), prod);
@@ -139,8 +140,8 @@ __global__ void __launch_bounds__(kAdRedThreads) k_ad_step(int n, const float4 *
     const float4 p = xs[s];
     const int na = A.nnz[s];
     for (int t = 0; t < na; t++) {
-      const double a = A.v[(size_t)t * n + s];
-      const float4 q = y[A.j[(size_t)t * n + s]];
+      const double a = A.v[(size_t)s * A.ld + t];
+      const float4 q = y[A.j[(size_t)s * A.ld + t]];
       const double yy[3] = {q.x, q.y, q.z};
       double u[3], u2[3], u3[3], u4[3];
       u[0] = w[1] * yy[2] - w[2] * yy[1] + vv[0];
@@ -286,8 +287,9 @@ int run_association_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const floa
   int rc = run_association_edges(h, {src}, {tgt}, {b.xs}, {0.f}, std::vector<float>(Q, Q + 12), {ell}, {kAdCap},
                                  kAdCap, &E, &K);
   if (rc) return rc;
-  std::vector<int> nz(n), jj((size_t)n * kAdCap), sperm(n);
-  std::vector<float> vv((size_t)n * kAdCap);
+  const int ld = E[0].ld;
+  std::vector<int> nz(n), jj((size_t)n * ld), sperm(n);
+  std::vector<float> vv((size_t)n * ld);
   CVO_CUDA_TRY(h, cudaMemcpyAsync(nz.data(), E[0].nnz_row, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
   CVO_CUDA_TRY(h, cudaMemcpyAsync(jj.data(), E[0].A_j, sizeof(int) * jj.size(), cudaMemcpyDeviceToHost, h->stream));
   CVO_CUDA_TRY(h, cudaMemcpyAsync(vv.data(), E[0].A_v, sizeof(float) * vv.size(), cudaMemcpyDeviceToHost, h->stream));
@@ -302,7 +304,7 @@ int run_association_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const floa
   std::vector<std::pair<int, float>> row;
   for (int s = 0; s < n; s++) {
     row.clear();
-    for (int t = 0; t < nz[s]; t++) row.emplace_back(jj[(size_t)t * n + s], vv[(size_t)t * n + s]);
+    for (int t = 0; t < nz[s]; t++) row.emplace_back(jj[(size_t)s * ld + t], vv[(size_t)s * ld + t]);
     std::sort(row.begin(), row.end(), [](const std::pair<int, float> &a, const std::pair<int, float> &b2) {
       return a.first < b2.first;
     });
@@ -358,8 +360,8 @@ int run_align_adaptive(Handle *h, DevCloud *src, DevCloud *tgt, const float T_in
     int rc = run_association_edges(h, {src, src, tgt}, {tgt, src, tgt}, {b.xs, b.xs, b.ys}, {0.f, 0.f, 0.f}, poses,
                                    {ell, ell, ell}, {kAdCap, kAdCap, kAdCap}, kAdCap, &E, &K);
     if (rc) return rc;
-    const Ell A{E[0].A_j, E[0].A_v, E[0].nnz_row}, X{E[1].A_j, E[1].A_v, E[1].nnz_row};
-    const Ell Y{E[2].A_j, E[2].A_v, E[2].nnz_row};
+    const Ell A{E[0].A_j, E[0].A_v, E[0].nnz_row, E[0].ld}, X{E[1].A_j, E[1].A_v, E[1].nnz_row, E[1].ld};
+    const Ell Y{E[2].A_j, E[2].A_v, E[2].nnz_row, E[2].ld};
     k_ad_flow<<<bn, kAdRedThreads, 0, h->stream>>>(n, b.xs, src->pos, b.yo, A, X, p.c, p.d, ell, b.part);
     k_ad_flow_yy<<<bm, kAdRedThreads, 0, h->stream>>>(m, b.ys, b.yo, Y, ell, b.part + (size_t)9 * bn);
     h->launches += 2;

@@ -197,7 +197,8 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
   int cnt = 0;
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;
-  auto put = [&](int r, int slot, int j, float a) { put_kept(P, n, cap, ov, (size_t)(tile0 + r), slot, j, a); };
+  const int ld = P->ld;
+  auto put = [&](int r, int slot, int j, float a) { put_kept(P, ld, cap, ov, (size_t)(tile0 + r), slot, j, a); };
   // cells farther than the largest radius from every query point are skipped
   const float slack = 1e-3f * G.h;
   const float prune_r2 = (brq + slack) * (brq + slack);

@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
     float coef = __double2float_rn(__ddiv_rn(1.0, dm(dm(2.0, (double)tl), (double)tl)));
     const int z = P->nnz_row[s];
     const float4 *__restrict__ yorig = P->yorig;
-    const int *__restrict__ Aj = P->A_j + s;
-    const float *__restrict__ Av = P->A_v + s;
+    const int *__restrict__ Aj = P->A_j + (size_t)s * P->ld;
+    const float *__restrict__ Av = P->A_v + (size_t)s * P->ld;
     auto add = [&](float a, const float4 &y) {
       float ux = w1 * y.z - w2 * y.y + u0v, uy = w2 * y.x - w0 * y.z + u1v, uz = w0 * y.y - w1 * y.x + u2v;
       float px = w1 * uz - w2 * uy, py = w2 * ux - w0 * uz, pz = w0 * uy - w1 * ux;          // xi^2 z
@@ -257,19 +257,17 @@ __global__ void __launch_bounds__(kStepThreads) k_step(BatchDev B, KParams K, co
       Es += a * (epsil + beta * delta + 0.5f * b2 * gamma + 0.5f * gamma * gamma + b2 * b2 * (1.f / 24.f));
     };
     int c = 0;
-    // four entries' loads in flight at a time; the sums keep slot order
+    // four entries per 16-byte load (rows are 16-byte aligned); the sums keep slot order
     for (; c + 4 <= z; c += 4) {
-      const int j0 = Aj[(size_t)c * n], j1 = Aj[(size_t)(c + 1) * n], j2 = Aj[(size_t)(c + 2) * n],
-                j3 = Aj[(size_t)(c + 3) * n];
-      const float a0 = Av[(size_t)c * n], a1 = Av[(size_t)(c + 1) * n], a2 = Av[(size_t)(c + 2) * n],
-                  a3 = Av[(size_t)(c + 3) * n];
-      const float4 y0 = __ldg(&yorig[j0]), y1 = __ldg(&yorig[j1]), y2 = __ldg(&yorig[j2]), y3 = __ldg(&yorig[j3]);
-      add(a0, y0);
-      add(a1, y1);
-      add(a2, y2);
-      add(a3, y3);
+      const int4 j4 = *reinterpret_cast<const int4 *>(Aj + c);
+      const float4 a4 = *reinterpret_cast<const float4 *>(Av + c);
+      const float4 y0 = __ldg(&yorig[j4.x]), y1 = __ldg(&yorig[j4.y]), y2 = __ldg(&yorig[j4.z]), y3 = __ldg(&yorig[j4.w]);
+      add(a4.x, y0);
+      add(a4.y, y1);
+      add(a4.z, y2);
+      add(a4.w, y3);
     }
-    for (; c < z; c++) add(Av[(size_t)c * n], __ldg(&yorig[Aj[(size_t)c * n]]));
+    for (; c < z; c++) add(Av[c], __ldg(&yorig[Aj[c]]));
   }
   double v[4] = {Bs, Cs, Ds, Es};
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -308,8 +306,8 @@ __global__ void k_export(const PairDev *P, const int *row_start, int *cols, floa
   int z = P->nnz_row[s];
   int o = row_start[s];
   for (int c = 0; c < z; c++) {
-    cols[o + c] = P->A_j[(size_t)c * P->n + s];
-    vals[o + c] = P->A_v[(size_t)c * P->n + s];
+    cols[o + c] = P->A_j[(size_t)s * P->ld + c];
+    vals[o + c] = P->A_v[(size_t)s * P->ld + c];
   }
 }
 
@@ -564,6 +562,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   int ov = kSelMax;
   if (rows_all > 0) ov = (int)std::min<long long>(ov, (8ll << 30) / (8ll * rows_all));
   bh->ov = ov;
+  const int ell_ld = (std::max(capmax, 1) + 3) & ~3;   // 16-byte aligned ELL rows
   for (int p = 0; p < np; p++) {
     int n = srcs[p]->n, m = tgts[p]->n;
     // tiles per pair padded to whole association blocks (kCtaWarps tiles of one pair)
@@ -576,8 +575,8 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     max_part_blocks = std::max(max_part_blocks, std::max(rb, sb));
     add(sizeof(float4) * m);                                     // ycur
     add(sizeof(float4) * m);                                     // yorig
-    add(sizeof(int) * (size_t)n * capmax);                       // ELL (every mode: the row selection uses it)
-    add(sizeof(float) * (size_t)n * capmax);
+    add(sizeof(int) * (size_t)n * ell_ld);                       // ELL (every mode: the row selection uses it)
+    add(sizeof(float) * (size_t)n * ell_ld);
     add(sizeof(int2) * (size_t)n * ov);                          // spill lists
     add(sizeof(int) * n);                                        // nnz_row
     add(sizeof(float) * 8 * (size_t)n);                          // row_sums
@@ -610,8 +609,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     P.xs = s->spos; P.xf = s->sfeat; P.xl = s->slab; P.xg = s->sgeo; P.sperm = s->sperm;
     P.ycur = ar.take<float4>(t->n);
     P.yorig = ar.take<float4>(t->n);
-    P.A_j = ar.take<int>((size_t)s->n * capmax);
-    P.A_v = ar.take<float>((size_t)s->n * capmax);
+    P.A_j = ar.take<int>((size_t)s->n * ell_ld);
+    P.A_v = ar.take<float>((size_t)s->n * ell_ld);
+    P.ld = ell_ld;
     P.ovf = ar.take<int2>((size_t)s->n * ov);
     P.ov = ov;
     P.tf = t->feat; P.tl = t->lab; P.tg = t->geo;
@@ -1067,6 +1067,7 @@ int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const 
     const PairDev &P = bh.pairs[e];
     EdgeAssoc &A = (*out)[e];
     A.A_j = P.A_j; A.A_v = P.A_v; A.nnz_row = P.nnz_row;
+    A.ld = P.ld;
     A.n = P.n; A.m = P.m;
     A.nnz = P.done ? 0 : P.nnz_sum;
     A.max_row = P.done ? 0 : P.max_row;

@@ -104,8 +104,9 @@ struct PairDev {
   float level_r[24];              // largest search radius each level serves
   float4 *ycur;                   // transformed targets, current level order
   float4 *yorig;                  // transformed targets, original order
-  int *A_j; float *A_v;           // ELL, slot-major: entry c of row s at [c * n + s] (original target index)
-  int2 *ovf;                      // row lists: kept pair t of row s at [s * ov + t] = {j, bits of a}
+  int *A_j; float *A_v;           // ELL, row-major: entry c of row s at [s * ld + c] (original target index)
+  int ld;                         // ELL row pitch (capmax rounded up to a multiple of 4)
+  int2 *ovf;                      // spill lists: kept pair cap + t of row s at [s * ov + t] = {j, bits of a}
   int ov;                         // row-list entries per row
   const float *tf, *tl;           // target features / labels, original order (float4 chunks)
   const float2 *tg;               // target geometric types, original order
@@ -262,8 +263,9 @@ int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, cons
 // pose (row-major 3x4, frame -> world) applied to the target points.  The result
 // arrays stay valid until the next batch is built on the handle.
 struct EdgeAssoc {
-  const int *A_j;        // ELL, slot-major over tile-ordered rows, original target indices
+  const int *A_j;        // ELL, row-major over tile-ordered rows (pitch ld), original target indices
   const float *A_v;
+  int ld;
   const int *nnz_row;
   int n, m;
   long long nnz;

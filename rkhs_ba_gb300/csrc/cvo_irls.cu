@@ -41,9 +41,10 @@ __global__ void k_world(const float4 *local, int n, const float *pose, float4 *w
 }
 
 struct IrlsEdge {
-  const int *A_j;
+  const int *A_j;     // ELL, row-major with pitch ld
   const float *A_v;
   const int *nnz_row;
+  int ld;
   const float4 *p1;   // frame-1 local points, tile order (rows of A)
   const float4 *p2;   // frame-2 local points, original order (columns of A)
   int n, lim;         // rows, entries used per row
@@ -77,8 +78,8 @@ __global__ void __launch_bounds__(kIrlsThreads) k_irls_accum(const IrlsEdge *E, 
     double q1[3];
     for (int r = 0; r < 3; r++) q1[r] = T1[4 * r] * p1[0] + T1[4 * r + 1] * p1[1] + T1[4 * r + 2] * p1[2] + T1[4 * r + 3];
     for (int c = 0; c < z; c++) {
-      const int j = ed.A_j[(size_t)c * ed.n + s];
-      const double a = ed.A_v[(size_t)c * ed.n + s];
+      const int j = ed.A_j[(size_t)s * ed.ld + c];
+      const double a = ed.A_v[(size_t)s * ed.ld + c];
       const float4 b2 = __ldg(&ed.p2[j]);
       const double p2[3] = {b2.x, b2.y, b2.z};
       double ev[3];
@@ -422,6 +423,7 @@ int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, c
       if (EA[e].nnz != 0 && EA[e].nnz >= p.multiframe_min_nonzeros) {
         IrlsEdge E;
         E.A_j = EA[e].A_j; E.A_v = EA[e].A_v; E.nnz_row = EA[e].nnz_row;
+        E.ld = EA[e].ld;
         E.p1 = clouds[edges[2 * e]]->spos;
         E.p2 = clouds[edges[2 * e + 1]]->pos;
         E.n = EA[e].n;

@@ -321,10 +321,10 @@ __device__ __forceinline__ void finish_row(const BatchDev &B, PairDev *P, int p,
 
 // Stores kept pair number `slot` of source row sidx: the first cap go to the row's
 // ELL slots, the next ov to its spill list (row-major), the rest are only counted.
-__device__ __forceinline__ void put_kept(PairDev *P, int n, int cap, int ov, size_t sidx, int slot, int j, float a) {
+__device__ __forceinline__ void put_kept(PairDev *P, int ld, int cap, int ov, size_t sidx, int slot, int j, float a) {
   if (slot < cap) {
-    P->A_j[(size_t)slot * n + sidx] = j;
-    P->A_v[(size_t)slot * n + sidx] = a;
+    P->A_j[sidx * ld + slot] = j;
+    P->A_v[sidx * ld + slot] = a;
   } else if (slot - cap < ov) {
     P->ovf[sidx * ov + (slot - cap)] = make_int2(j, __float_as_int(a));
   }
@@ -608,7 +608,8 @@ __device__ __forceinline__ void assoc_warp(const BatchDev &B, const KParams &K, 
   const int ov = P->ov;
   const int tile0 = (gw - B.tile_off[p]) * 32;   // source index of lane 0's row
   // kept pair number `slot` of row r enters its ELL slot (first cap) or its spill list
-  auto put = [&](int r, int slot, int j, float a) { put_kept(P, n, cap, ov, (size_t)(tile0 + r), slot, j, a); };
+  const int ld = P->ld;
+  auto put = [&](int r, int slot, int j, float a) { put_kept(P, ld, cap, ov, (size_t)(tile0 + r), slot, j, a); };
   for (int pass = 0; pass < npass; pass++) {
     int x0, y0, z0, nx, ny, nz;
     bool me = valid;
@@ -727,12 +728,12 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
   const int p = find_segment(B.row_off, B.npairs, g);
   const PairDev *P = &B.pairs[p];
   if (P->done) return;
-  const int s = g - B.row_off[p], n = P->n;
+  const int s = g - B.row_off[p];
   const int z = P->nnz_row[s];
   const float4 x = __ldg(&P->xs[s]);
   float w0 = 0.f, w1 = 0.f, w2 = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, as = 0.f;
-  const int *__restrict__ Aj = P->A_j + s;
-  const float *__restrict__ Av = P->A_v + s;
+  const int *__restrict__ Aj = P->A_j + (size_t)s * P->ld;
+  const float *__restrict__ Av = P->A_v + (size_t)s * P->ld;
   const float4 *__restrict__ yorig = P->yorig;
   auto add = [&](float a, const float4 &y) {
     w0 = fmaf(a, fs(fm(x.y, y.z), fm(x.z, y.y)), w0);
@@ -744,19 +745,17 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
     as += a;
   };
   int c = 0;
-  // four entries' loads in flight at a time; the sums keep slot order
+  // four entries per 16-byte load (rows are 16-byte aligned); the sums keep slot order
   for (; c + 4 <= z; c += 4) {
-    const int j0 = Aj[(size_t)c * n], j1 = Aj[(size_t)(c + 1) * n], j2 = Aj[(size_t)(c + 2) * n],
-              j3 = Aj[(size_t)(c + 3) * n];
-    const float a0 = Av[(size_t)c * n], a1 = Av[(size_t)(c + 1) * n], a2 = Av[(size_t)(c + 2) * n],
-                a3 = Av[(size_t)(c + 3) * n];
-    const float4 y0 = __ldg(&yorig[j0]), y1 = __ldg(&yorig[j1]), y2 = __ldg(&yorig[j2]), y3 = __ldg(&yorig[j3]);
-    add(a0, y0);
-    add(a1, y1);
-    add(a2, y2);
-    add(a3, y3);
+    const int4 j4 = *reinterpret_cast<const int4 *>(Aj + c);
+    const float4 a4 = *reinterpret_cast<const float4 *>(Av + c);
+    const float4 y0 = __ldg(&yorig[j4.x]), y1 = __ldg(&yorig[j4.y]), y2 = __ldg(&yorig[j4.z]), y3 = __ldg(&yorig[j4.w]);
+    add(a4.x, y0);
+    add(a4.y, y1);
+    add(a4.z, y2);
+    add(a4.w, y3);
   }
-  for (; c < z; c++) add(Av[(size_t)c * n], __ldg(&yorig[Aj[(size_t)c * n]]));
+  for (; c < z; c++) add(Av[c], __ldg(&yorig[Aj[c]]));
   write_row_sums(P->row_sums + (size_t)s * 8, P->mode, K, w0, w1, w2, v0, v1, v2, as);
 }
 
@@ -783,13 +782,13 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
     const int4 it = B.sel_list[e];
     const PairDev *P = &B.pairs[it.x];
-    const int s = it.y, n = P->n, cap = P->cap, ov = P->ov;
+    const int s = it.y, cap = P->cap, ov = P->ov;
     const int E = it.z;
     const int2 *lst = P->ovf + (size_t)s * ov;
-    int *Aj = P->A_j + s;
-    float *Av = P->A_v + s;
+    int *Aj = P->A_j + (size_t)s * P->ld;
+    float *Av = P->A_v + (size_t)s * P->ld;
     const bool staged = E <= kSelStage;
-    auto gidx = [&](int t) -> int { return t < cap ? Aj[(size_t)t * n] : lst[t - cap].x; };
+    auto gidx = [&](int t) -> int { return t < cap ? Aj[t] : lst[t - cap].x; };
     int jmin = 0x7FFFFFFF, jmax = -1;
     for (int t = lane; t < E; t += 32) {
       const int j = gidx(t);
@@ -850,13 +849,13 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       if (t < E) {
         j = entry(t);
         k = j <= r;
-        if (k) a = t < cap ? Av[(size_t)t * n] : __int_as_float(lst[t - cap].y);
+        if (k) a = t < cap ? Av[t] : __int_as_float(lst[t - cap].y);
       }
       const unsigned bal = __ballot_sync(FULLMASK, k);
       const int c = base + __popc(bal & ((1u << lane) - 1u));
       if (k && c < cap) {
-        Aj[(size_t)c * n] = j;
-        Av[(size_t)c * n] = a;
+        Aj[c] = j;
+        Av[c] = a;
       }
       base += __popc(bal);
     }
@@ -875,7 +874,7 @@ __global__ void __launch_bounds__(kSelThreads) k_rescan(BatchDev B, KParams K) {
   for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
     const int4 it = B.scan_list[e];
     const PairDev *P = &B.pairs[it.x];
-    const int s = it.y, n = P->n, m = P->m, cap = P->cap, F = P->F, C = P->C;
+    const int s = it.y, m = P->m, cap = P->cap, F = P->F, C = P->C;
     const float4 x = P->xs[s];
     float4 xf[FCH > 0 ? FCH : 1];
     float4 xl[LCH > 0 ? LCH : 1];
@@ -904,8 +903,8 @@ __global__ void __launch_bounds__(kSelThreads) k_rescan(BatchDev B, KParams K) {
       if (k) {
         const int c = taken + __popc(bal & ((1u << lane) - 1u));
         if (c < cap) {
-          P->A_j[(size_t)c * n + s] = j;
-          P->A_v[(size_t)c * n + s] = a;
+          P->A_j[(size_t)s * P->ld + c] = j;
+          P->A_v[(size_t)s * P->ld + c] = a;
         }
       }
       taken += __popc(bal);
