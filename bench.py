@@ -400,7 +400,8 @@ def run_ours(args):
                 "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
                 "kernel": "k_assoc_cta + k_select + k_rescan + k_rowsum", "launches": prof["assoc_launches"],
                 "avg_launch_us": round(avg_s * 1e6, 3), "algorithmic_bytes_per_launch": round(per_launch_bytes),
-                "iteration_kernel_ms": {k: round(v, 3) for k, v in prof["kernel_ms"].items()}}
+                "iteration_kernel_ms": {k: round(v, 3) for k, v in prof["kernel_ms"].items()},
+                "association_phase_ms": {k: round(v, 3) for k, v in prof.get("assoc_split_ms", {}).items()}}
         try:
             sms = torch.cuda.get_device_properties(local).multi_processor_count
         except Exception:

@@ -451,6 +451,9 @@ int cvo_profile_reset(cvo_handle *h);
 /* Accumulated event-timed milliseconds of the kernels of the align iterations:
  * [transform, association, reduction, step, all four]. */
 int cvo_profile_kernels(const cvo_handle *h, double ms[5]);
+/* The association phase of the same iterations split into [association kernel
+ * (with its work-item ordering), row selection (first cap by index), row sums]. */
+int cvo_profile_assoc_split(const cvo_handle *h, double ms[3]);
 /* Last CUDA error text recorded by the handle (empty if none). */
 const char *cvo_last_error(const cvo_handle *h);
 

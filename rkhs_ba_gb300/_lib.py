@@ -137,6 +137,7 @@ SIGNATURES = {
     "cvo_profile_read": (_i, [_P, _DP, C.POINTER(C.c_int64), _DP, C.POINTER(C.c_int64)]),
     "cvo_profile_reset": (_i, [_P]),
     "cvo_profile_kernels": (_i, [_P, _DP]),
+    "cvo_profile_assoc_split": (_i, [_P, _DP]),
     "cvo_inner_product_noalloc": (_i, [C.POINTER(CvoParamsC), C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _f,
                                        _P, _P]),
 }

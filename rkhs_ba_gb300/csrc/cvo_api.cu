@@ -346,6 +346,14 @@ extern "C" int cvo_profile_kernels(const cvo_handle *H, double ms[5]) try {
   return status_from_exception();
 }
 
+extern "C" int cvo_profile_assoc_split(const cvo_handle *H, double ms[3]) try {
+  if (!H || !ms) return CVO_ERR_INVALID_ARG;
+  for (int k = 0; k < 3; k++) ms[k] = H->h.prof.assoc_split_ms[k];
+  return CVO_OK;
+} catch (...) {
+  return status_from_exception();
+}
+
 extern "C" int cvo_profile_reset(cvo_handle *H) try {
   if (!H) return CVO_ERR_INVALID_ARG;
   bool on = H->h.prof.on;

@@ -724,7 +724,9 @@ inline void mark(Handle *h, const cudaEvent_t *ev, int k) {
   if (ev) cudaEventRecordWithFlags(ev[k], h->stream, cudaEventRecordExternal);
 }
 
-// ev (optional): 5 events bracketing transform, assoc, reduce, step.
+// ev (optional): 7 events: 0-4 bracket transform, association phase, reduce and step;
+// 5 and 6 split the association phase into the association kernel (+ item order),
+// the selection (k_select + k_rescan) and the row sums.
 void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEvent_t *ev = nullptr) {
   BatchDev &B = bh->B;
   mark(h, ev, 0);
@@ -735,8 +737,10 @@ void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEv
     k_order_items<<<1, 1024, 0, h->stream>>>(B.n_items, B.item_cost, B.item_order);
     h->launches++;
   }
+  mark(h, ev, 5);
   k_select<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
   bh->rescan<<<bh->sel_blocks, kSelThreads, 0, h->stream>>>(B, K);
+  mark(h, ev, 6);
   k_rowsum<<<std::max((B.total_rows + 255) / 256, 1), 256, 0, h->stream>>>(B, K);
   mark(h, ev, 2);
   k_reduce<<<std::max(B.total_rblocks, 1), kReduceThreads, 0, h->stream>>>(B, K);
@@ -841,7 +845,7 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
   long long before = h->launches;
   // with profiling on, every kernel launch of the chunk is bracketed by
   // event-record nodes of the graph
-  constexpr int kEv = 5;
+  constexpr int kEv = 7;
   std::vector<cudaEvent_t> pev;
   if (h->prof.on) {
     pev.resize(kEv * kChunk);
@@ -872,6 +876,13 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
             h->prof.kernel_ms[k] += ms;
             h->prof.kernel_ms[4] += ms;
           }
+        }
+        // association phase: kernel (ev 1 -> 5), selection (5 -> 6), row sums (6 -> 2)
+        const int split[4] = {1, 5, 6, 2};
+        for (int k = 0; k < 3; k++) {
+          float ms = 0.f;
+          if (cudaEventElapsedTime(&ms, pev[kEv * it + split[k]], pev[kEv * it + split[k + 1]]) == cudaSuccess)
+            h->prof.assoc_split_ms[k] += ms;
         }
         h->prof.assoc_launches++;
       }

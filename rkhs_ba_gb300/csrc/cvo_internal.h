@@ -177,6 +177,7 @@ struct Profile {
   bool on = false;
   double assoc_ms = 0.0;
   double kernel_ms[5] = {0, 0, 0, 0, 0};   // transform, assoc, reduce, step, all four
+  double assoc_split_ms[3] = {0, 0, 0};    // association kernel, selection, row sums
   long long assoc_launches = 0;
   double assoc_bytes = 0.0;
   long long iterations = 0;

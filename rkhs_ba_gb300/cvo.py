@@ -226,8 +226,11 @@ class CvoGPU:
         k = (C.c_double * 5)()
         L.check(L.lib().cvo_profile_kernels(self._h, k), "cvo_profile_kernels")
         names = ("transform", "assoc", "reduce", "step", "iteration")
+        sp = (C.c_double * 3)()
+        L.check(L.lib().cvo_profile_assoc_split(self._h, sp), "cvo_profile_assoc_split")
         return {"assoc_ms": ms.value, "assoc_launches": n.value, "assoc_bytes": b.value, "iterations": it.value,
-                "kernel_ms": {names[i]: k[i] for i in range(5)}}
+                "kernel_ms": {names[i]: k[i] for i in range(5)},
+                "assoc_split_ms": {"kernel": sp[0], "select": sp[1], "rowsum": sp[2]}}
 
     def upload(self, cloud: CvoPointCloud) -> GpuCloud:
         return GpuCloud(self, cloud)
