@@ -715,8 +715,8 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
 }
 
 // ------------------------------------------------------------ selection
-constexpr int kSelMax = 4096;      // kept pairs beyond cap one spill list can hold
-constexpr int kSelStage = 2048;    // rows up to this many entries are selected from shared memory
+constexpr int kSelMax = 2048;      // kept pairs beyond cap one spill list can hold
+constexpr int kSelStage = 1024;    // rows up to this many entries are selected from shared memory
 constexpr int kSelThreads = 128;
 
 // Row partials of one source row from its final ELL entries, in slot order
@@ -761,21 +761,26 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
 
 // One warp per listed row with cap < count <= cap + ov: its ELL slots hold the
 // first cap kept pairs and its spill list (row-major) the rest, in the order they
-// were kept.  A radix select over d = j - jmin (jmin, jmax: the row's smallest and
-// largest kept index; 9-bit digits from the highest bit of jmax - jmin, warp-private
-// histograms in shared memory) finds the cap-th smallest index r.  Offsetting by jmin
-// spreads neighbouring indices over the bins, so the histogram atomics rarely collide
-// and a row whose indices span fewer than 512 values needs one pass.  The entries
-// with index <= r (exactly cap: indices are distinct) are compacted in list order
-// into the ELL slots, in place (an entry is read before any write can reach its slot).
-// Indices are staged in shared memory when the row fits (kSelStage entries).
+// were kept.  A row of up to kSelStage entries is first staged in shared memory
+// (indices and values, 16-byte loads: many loads in flight per lane), so the rest
+// of the selection touches global memory only to write the result.  A radix select
+// over d = j - jmin (jmin, jmax: the row's smallest and largest kept index; 9-bit
+// digits from the highest bit of jmax - jmin, warp-private histograms) finds the
+// cap-th smallest index r.  Offsetting by jmin spreads neighbouring indices over the
+// bins, so the histogram atomics rarely collide and a row whose indices span fewer
+// than 512 values needs one pass.  The entries with index <= r (exactly cap: indices
+// are distinct) are compacted in list order into the ELL slots.  Longer rows read
+// their entries from global memory on every pass; the compaction is then in place
+// (an entry is read before any write can reach its slot).
 constexpr int kSelBins = 512;
 constexpr int kSelDigit = 9;
 __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
+  __shared__ float vbuf_all[kSelThreads / 32][kSelStage];
   __shared__ int hist_all[kSelThreads / 32][kSelBins];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *jb = jbuf_all[w];
+  float *vb = vbuf_all[w];
   int *hist = hist_all[w];
   const int count = *B.sel_count;
   const int nwarps = gridDim.x * (kSelThreads / 32);
@@ -790,11 +795,53 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     const bool staged = E <= kSelStage;
     auto gidx = [&](int t) -> int { return t < cap ? Aj[t] : lst[t - cap].x; };
     int jmin = 0x7FFFFFFF, jmax = -1;
-    for (int t = lane; t < E; t += 32) {
-      const int j = gidx(t);
-      if (staged) jb[t] = j;
-      jmin = min(jmin, j);
-      jmax = max(jmax, j);
+    if (staged) {
+      // ELL part: 4 entries per 16-byte load (rows are 16-byte aligned, the pitch covers
+      // the rounded-up chunk); spill part: 2 entries per load (rows start 16-byte aligned)
+      const int nq = (cap + 3) >> 2;
+#pragma unroll 4
+      for (int q = lane; q < nq; q += 32) {
+        const int4 j4 = reinterpret_cast<const int4 *>(Aj)[q];
+        const float4 a4 = reinterpret_cast<const float4 *>(Av)[q];
+        const int jv[4] = {j4.x, j4.y, j4.z, j4.w};
+        const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (4 * q + i < cap) {
+            jb[4 * q + i] = jv[i];
+            vb[4 * q + i] = av[i];
+            jmin = min(jmin, jv[i]);
+            jmax = max(jmax, jv[i]);
+          }
+      }
+      const int ns = E - cap, np = (ns + 1) >> 1;
+#pragma unroll 4
+      for (int q = lane; q < np; q += 32) {
+        int2 e0, e1 = make_int2(0, 0);
+        if (2 * q + 1 < ns) {
+          const int4 v = reinterpret_cast<const int4 *>(lst)[q];
+          e0 = make_int2(v.x, v.y);
+          e1 = make_int2(v.z, v.w);
+        } else {
+          e0 = lst[2 * q];
+        }
+        jb[cap + 2 * q] = e0.x;
+        vb[cap + 2 * q] = __int_as_float(e0.y);
+        jmin = min(jmin, e0.x);
+        jmax = max(jmax, e0.x);
+        if (2 * q + 1 < ns) {
+          jb[cap + 2 * q + 1] = e1.x;
+          vb[cap + 2 * q + 1] = __int_as_float(e1.y);
+          jmin = min(jmin, e1.x);
+          jmax = max(jmax, e1.x);
+        }
+      }
+    } else {
+      for (int t = lane; t < E; t += 32) {
+        const int j = gidx(t);
+        jmin = min(jmin, j);
+        jmax = max(jmax, j);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -849,7 +896,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       if (t < E) {
         j = entry(t);
         k = j <= r;
-        if (k) a = t < cap ? Av[t] : __int_as_float(lst[t - cap].y);
+        if (k) a = staged ? vb[t] : (t < cap ? Av[t] : __int_as_float(lst[t - cap].y));
       }
       const unsigned bal = __ballot_sync(FULLMASK, k);
       const int c = base + __popc(bal & ((1u << lane) - 1u));
