@@ -376,6 +376,10 @@ int cvo_proposal_dims(const cvo_proposal *p, int *num_params, int *points_per_cl
 int cvo_proposal_get(cvo_handle *h, cvo_proposal *p, int which, float *out);
 /* new weights (num_params floats); the Adam state restarts */
 int cvo_proposal_set(cvo_handle *h, cvo_proposal *p, const float *weights);
+/* Which kernel computes the network's matrix products: 0 (default) the tcgen05
+ * tensor-core GEMM with TMEM accumulators, 1 the warp-level mma.sync GEMM (kept as a
+ * second opinion for tests).  No reference counterpart. */
+int cvo_proposal_set_gemm(cvo_proposal *p, int kind);
 /* One training step on n_pairs labelled pairs drawn from a device-resident pool:
  * src_pts / tgt_pts are device arrays of n_scenes x n_pts x 8 floats (x, y, z and
  * 5 features); pair b takes scene[b] and moves its target by T_label[b] (12 floats,

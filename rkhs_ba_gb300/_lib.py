@@ -120,6 +120,7 @@ SIGNATURES = {
     "cvo_proposal_dims": (_i, [_P, _IP, _IP, _IP]),
     "cvo_proposal_get": (_i, [_P, _P, _i, _FP]),
     "cvo_proposal_set": (_i, [_P, _P, _FP]),
+    "cvo_proposal_set_gemm": (_i, [_P, _i]),
     "cvo_proposal_train_pool_dev": (_i, [_P, _P, _i, _i, _P, _P, _i, _IP, _FP, _f, C.c_uint32, _FP]),
     "cvo_proposal_forward_pool_dev": (_i, [_P, _P, _i, _i, _P, _P, _i, _IP, _FP, C.c_uint32, _FP, _FP]),
     "cvo_proposal_hypotheses_dev": (_i, [_P, _P, _i, C.POINTER(_P), C.POINTER(_P), C.c_uint32, _FP]),

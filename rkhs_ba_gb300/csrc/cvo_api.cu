@@ -1225,6 +1225,13 @@ extern "C" int cvo_proposal_set(cvo_handle *H, cvo_proposal *p, const float *wei
   return status_from_exception();
 }
 
+extern "C" int cvo_proposal_set_gemm(cvo_proposal *p, int kind) try {
+  if (!p) return CVO_ERR_INVALID_ARG;
+  return net_set_gemm(p->n, kind);
+} catch (...) {
+  return status_from_exception();
+}
+
 extern "C" int cvo_proposal_train_pool_dev(cvo_handle *H, cvo_proposal *p, int n_scenes, int n_pts,
                                            const float *src_pts, const float *tgt_pts, int n_pairs, const int *scene,
                                            const float *T_label, float lr, uint32_t seed, float *loss) try {

@@ -39,6 +39,7 @@ struct __align__(16) CtaDense {
   long long lred[kCtaWarps][2];
   int ired[kCtaWarps][2];
   int okg[kCtaCand / 32];
+  int gcnt[kCtaWarps][32];                   // split items: kept pairs per row and candidate group
   GridDesc G;
 };
 
@@ -72,19 +73,30 @@ __device__ __forceinline__ int block_excl_scan(int v, int &excl, int (*scratch)[
   return total;
 }
 
-// One work item: the four tiles gw0 .. gw0 + 3 (one pair).
+// One work item: the four tiles gw0 .. gw0 + 3 (one pair), each warp owning one tile.
+// split >= 0 (a heavy item, split by k_order_items): only tile gw0 + split, with the
+// four warps sharing its candidate stream -- warp w evaluates candidate group w of
+// every 128-candidate step for the tile's 32 rows.  The kept pairs of a row are then
+// placed in the order (step, group, candidate) exactly as one warp would place them:
+// each warp counts its group's kept pairs per row, and after a block barrier writes
+// them behind the counts of the lower groups (a second, identical evaluation of its
+// survivors).  So the kernel matrix and the order of every row's entries do not
+// depend on which items are split.
 template <int FCH, int LCH, bool GT>
-__device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K, int gw0, unsigned char *cta_smem) {
+__device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K, int gw0, int split,
+                                            unsigned char *cta_smem) {
   using D = CtaDense<FCH, LCH, GT>;
   constexpr int FP = D::FP, LP = D::LP;
   D &sm = *reinterpret_cast<D *>(cta_smem);
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-  const int gw = gw0 + wib;
+  const int gw = gw0 + (split >= 0 ? split : wib);
+  // the per-warp fallback runs once per tile: in a split item only warp 0 takes it
+  const bool fallback_warp = split < 0 || wib == 0;
   const int p = find_segment(B.tile_off, B.npairs, gw0);
   PairDev *P = &B.pairs[p];
   if (P->done) return;
   if (!K.use_mma || P->F > 8) {
-    assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
+    if (fallback_warp) assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
     return;
   }
   const int n = P->n;
@@ -169,7 +181,7 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
   const bool dense = union_ok && !(ucells > 64 && ucells > 2 * own_sum) && ucells <= 2 * warp_cells;
   __syncthreads();
   if (!dense) {
-    assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
+    if (fallback_warp) assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
     return;
   }
   // ---- dense: prefilter vectors of the rows around the block's centre
@@ -191,7 +203,7 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
 #pragma unroll
   for (int q = 0; q < LP; q++) sr.l[lane * LP + q] = xl[q];
   if (!__syncthreads_and(okA)) {
-    assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
+    if (fallback_warp) assoc_warp<FCH, LCH, GT>(B, K, gw, cta_smem);
     return;
   }
   int cnt = 0;
@@ -269,16 +281,45 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
       }
       __syncthreads();
       const int nk = min(kCtaCand, lcands - st0);
+      if (split < 0) {
 #pragma unroll 1
-      for (int g = 0; g < kCtaCand / 32; g++) {
-        const int gk = nk - 32 * g;
-        if (gk <= 0) break;
-        uint32_t cand = sm.okg[g] ? mma_filter(&sm.apl[wib][0][0], 32, &sm.bpl[0][32 * g], kCtaCand, lane, K.mma_tau)
-                                  : 0xFFFFFFFFu;
-        cand &= gk >= 32 ? 0xFFFFFFFFu : ((1u << gk) - 1u);
-        if (!valid) cand = 0u;
-        eval_survivors<FCH, LCH, GT>(K, F, C, lane, cand, cnt, sr, sm.pos + 32 * g, sm.feat + 32 * g * FP,
+        for (int g = 0; g < kCtaCand / 32; g++) {
+          const int gk = nk - 32 * g;
+          if (gk <= 0) break;
+          uint32_t cand = sm.okg[g] ? mma_filter(&sm.apl[wib][0][0], 32, &sm.bpl[0][32 * g], kCtaCand, lane, K.mma_tau)
+                                    : 0xFFFFFFFFu;
+          cand &= gk >= 32 ? 0xFFFFFFFFu : ((1u << gk) - 1u);
+          if (!valid) cand = 0u;
+          eval_survivors<FCH, LCH, GT>(K, F, C, lane, cand, cnt, sr, sm.pos + 32 * g, sm.feat + 32 * g * FP,
+                                       sm.lab + 32 * g * LP, sm.geo + (GT ? 32 * g : 0), put);
+        }
+      } else {
+        const int g = wib, gk = nk - 32 * g;
+        uint32_t cand = 0u;
+        if (gk > 0) {
+          cand = sm.okg[g] ? mma_filter(&sm.apl[wib][0][0], 32, &sm.bpl[0][32 * g], kCtaCand, lane, K.mma_tau)
+                           : 0xFFFFFFFFu;
+          cand &= gk >= 32 ? 0xFFFFFFFFu : ((1u << gk) - 1u);
+          if (!valid) cand = 0u;
+        }
+        // pass 1: kept pairs per row in this group (nothing stored)
+        int kept = 0;
+        auto count_only = [](int, int, int, float) {};
+        eval_survivors<FCH, LCH, GT>(K, F, C, lane, cand, kept, sr, sm.pos + 32 * g, sm.feat + 32 * g * FP,
+                                     sm.lab + 32 * g * LP, sm.geo + (GT ? 32 * g : 0), count_only);
+        sm.gcnt[g][lane] = kept;
+        __syncthreads();
+        int base = cnt, total = cnt;
+#pragma unroll
+        for (int q = 0; q < kCtaWarps; q++) {
+          const int c = sm.gcnt[q][lane];
+          if (q < g) base += c;
+          total += c;
+        }
+        // pass 2: the same survivors, stored behind the lower groups' pairs
+        eval_survivors<FCH, LCH, GT>(K, F, C, lane, cand, base, sr, sm.pos + 32 * g, sm.feat + 32 * g * FP,
                                      sm.lab + 32 * g * LP, sm.geo + (GT ? 32 * g : 0), put);
+        cnt = total;
       }
       __syncthreads();
     }
@@ -286,58 +327,88 @@ __device__ __forceinline__ void assoc_block(const BatchDev &B, const KParams &K,
     lcands = 0;
     if (ci0 >= ucells) break;
   }
-  if (valid) finish_row(B, P, p, s, cnt, cap, P->ov);
+  if (valid && fallback_warp) finish_row(B, P, p, s, cnt, cap, P->ov);
 }
 
-// Persistent blocks take work items (four tiles each) from a counter, so blocks
-// that finish early pick up the remaining tiles.
+// Persistent blocks take work items from a counter, so blocks that finish early pick
+// up the remaining ones.  An entry of the item order is (item << 3) | mode: mode 4 runs
+// the item's four tiles (one per warp), modes 0-3 one tile of a split item.  Thread 0
+// adds the SM clock cycles an entry took (>> 8) to its item's cost.
+constexpr int kItemWhole = 4;
+
 template <int FCH, int LCH, bool GT>
 __global__ void __launch_bounds__(kCtaRows, 4) k_assoc_cta(BatchDev B, KParams K) {
   extern __shared__ __align__(128) unsigned char cta_smem[];
   __shared__ int item;
-  const int items = B.total_warps / kCtaWarps;
+  const int entries = *B.n_order;
   int last = -1;
   long long t0 = 0;
   while (true) {
     __syncthreads();   // every thread has finished the previous item; shared memory is free
     if (threadIdx.x == 0) {
-      if (last >= 0) B.item_cost[last] = (int)min((clock64() - t0) >> 8, 0x7FFFFFFFLL);
+      if (last >= 0) atomicAdd(&B.item_cost[last], (int)min((clock64() - t0) >> 8, 0x3FFFFFFFLL));
       item = atomicAdd(B.assoc_next, 1);
     }
     __syncthreads();
     const int it = item;
-    if (it >= items) break;
-    const int wi = B.item_order[it];
+    if (it >= entries) break;
+    const int code = B.item_order[it];
+    const int wi = code >> 3, mode = code & 7;
     if (threadIdx.x == 0) {
       last = wi;
       t0 = clock64();
     }
-    assoc_block<FCH, LCH, GT>(B, K, wi * kCtaWarps, cta_smem);
+    assoc_block<FCH, LCH, GT>(B, K, wi * kCtaWarps, mode == kItemWhole ? -1 : mode, cta_smem);
   }
 }
 
-// Orders the work items for the next pass: descending buckets of log2 cost (one block;
-// the order inside a bucket is arbitrary and does not change any result).
-__global__ void __launch_bounds__(1024) k_order_items(int n, const int *cost, int *order) {
-  __shared__ int hist[33], off[33];
-  for (int b = threadIdx.x; b < 33; b += blockDim.x) hist[b] = 0;
+__device__ __forceinline__ int cost_bucket(long long c) { return c > 0 ? min(63 - __clzll(c), 32) + 1 : 0; }
+
+// Orders the work items for the next pass (one block) from the cost each took in this
+// one, and resets the costs.  An item that cost more than one block's fair share of
+// the pass (total / blocks) cannot finish with the rest of the pass; it is split into
+// its four tiles, each run by a whole block (estimated 3/8 of the item's cost each:
+// a quarter of the work plus the counting pass).  Entries are placed in descending
+// buckets of log2 cost; the order inside a bucket is arbitrary and, like the split,
+// changes no result.
+__global__ void __launch_bounds__(1024) k_order_items(int n, int blocks, int *cost, int *order, int *n_order) {
+  __shared__ int hist[34], off[34];
+  __shared__ long long wsum[32];
+  long long t = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += cost[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULLMASK, t, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = t;
+  for (int b = threadIdx.x; b < 34; b += blockDim.x) hist[b] = 0;
   __syncthreads();
+  long long total = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) total += wsum[w];
+  const long long share = blocks > 0 ? total / blocks : 0;
+  auto is_split = [&](long long c) { return share > 0 && c > share; };
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int c = cost[i];
-    atomicAdd(&hist[c > 0 ? 32 - __clz(c) : 0], 1);
+    const long long c = cost[i];
+    if (is_split(c)) atomicAdd(&hist[cost_bucket(c * 3 / 8)], kCtaWarps);
+    else atomicAdd(&hist[cost_bucket(c)], 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int run = 0;
-    for (int b = 32; b >= 0; b--) {
+    for (int b = 33; b >= 0; b--) {
       off[b] = run;
       run += hist[b];
     }
+    *n_order = run;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int c = cost[i];
-    order[atomicAdd(&off[c > 0 ? 32 - __clz(c) : 0], 1)] = i;
+    const long long c = cost[i];
+    if (is_split(c)) {
+      const int at = atomicAdd(&off[cost_bucket(c * 3 / 8)], kCtaWarps);
+      for (int q = 0; q < kCtaWarps; q++) order[at + q] = (i << 3) | q;
+    } else {
+      order[atomicAdd(&off[cost_bucket(c)], 1)] = (i << 3) | kItemWhole;
+    }
+    cost[i] = 0;
   }
 }
 

@@ -593,8 +593,9 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   add(sizeof(int4) * (size_t)total_rows);                        // selection list
   add(sizeof(int4) * (size_t)total_rows);                        // rescan list
   const int n_items = bh->tile_off[np] / kCtaWarps;
-  add(sizeof(int) * (size_t)std::max(n_items, 1));               // work-item order
+  add(sizeof(int) * (size_t)std::max(n_items, 1) * kCtaWarps);   // work-item order (split items: 4 entries)
   add(sizeof(int) * (size_t)std::max(n_items, 1));               // work-item cost
+  add(sizeof(int));                                              // entries of the order
   if ((rc = ensure_workspace(h, bytes))) return rc;
   Arena ar;
   ar.base = h->ws->dev;
@@ -657,14 +658,18 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   bh->src_max_norm = ar.take<float>(np);
   int4 *sel_list_d = ar.take<int4>(total_rows);
   int4 *scan_list_d = ar.take<int4>(total_rows);
-  int *item_order_d = ar.take<int>((size_t)std::max(n_items, 1));
+  int *item_order_d = ar.take<int>((size_t)std::max(n_items, 1) * kCtaWarps);
   int *item_cost_d = ar.take<int>((size_t)std::max(n_items, 1));
+  int *n_order_d = ar.take<int>(1);
   {
+    // first pass: every item whole, in index order
     std::vector<int> ord(std::max(n_items, 1));
-    for (int i = 0; i < (int)ord.size(); i++) ord[i] = i;
+    for (int i = 0; i < (int)ord.size(); i++) ord[i] = (i << 3) | kItemWhole;
     CVO_CUDA_TRY(h, cudaMemcpyAsync(item_order_d, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice,
                                     h->stream));
     CVO_CUDA_TRY(h, cudaMemsetAsync(item_cost_d, 0, sizeof(int) * ord.size(), h->stream));
+    const int n_ord = n_items;
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(n_order_d, &n_ord, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   }
   // zero counters of every pair
   for (int p = 0; p < np; p++) CVO_CUDA_TRY(h, cudaMemsetAsync(bh->pairs[p].counter, 0, 2 * sizeof(unsigned), h->stream));
@@ -707,6 +712,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   B.n_items = n_items;
   B.item_order = item_order_d;
   B.item_cost = item_cost_d;
+  B.n_order = n_order_d;
   {
     int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
     B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
@@ -735,7 +741,8 @@ void launch_association(Handle *h, BatchHost *bh, const KParams &K, const cudaEv
   mark(h, ev, 1);
   bh->assoc<<<std::max(bh->assoc_blocks, 1), kAssocThreads, bh->assoc_smem, h->stream>>>(B, K);
   if (B.n_items > 1) {
-    k_order_items<<<1, 1024, 0, h->stream>>>(B.n_items, B.item_cost, B.item_order);
+    k_order_items<<<1, 1024, 0, h->stream>>>(B.n_items, std::max(bh->assoc_blocks, 1), B.item_cost, B.item_order,
+                                             B.n_order);
     h->launches++;
   }
   mark(h, ev, 5);

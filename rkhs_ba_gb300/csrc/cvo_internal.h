@@ -164,10 +164,12 @@ struct BatchDev {
   int *scan_count;
   int *assoc_next;                // next association work item (persistent blocks); reset by k_transform
   // work items (four tiles of one pair) in the order the persistent blocks take them:
-  // heaviest first by the cost each took in the previous pass (SM clock / 256)
+  // heaviest first by the cost each took in the previous pass (SM clock / 256); an
+  // entry is (item << 3) | mode, mode 4 = whole item, 0-3 = one tile of a split item
   int n_items;
-  int *item_order;
+  int *item_order;                // up to 4 n_items entries
   int *item_cost;
+  int *n_order;                   // entries of item_order
 };
 
 // ------------------------------------------------------------- host side
@@ -309,6 +311,7 @@ int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *s
                    const int *scene, const float *T_label, float lr, uint32_t seed, float *loss_out);
 int net_get(Handle *h, NetDev *n, int which, float *out);
 int net_set(Handle *h, NetDev *n, const float *in);
+int net_set_gemm(NetDev *n, int kind);
 
 // error helpers
 int set_cuda_error(Handle *h, cudaError_t e, const char *where);

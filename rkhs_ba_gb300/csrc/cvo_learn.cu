@@ -187,6 +187,213 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, int kc, 
       }
 }
 
+// ------------------------------------------------------- tcgen05 GEMM
+// The same product on the fifth-generation tensor cores: one CTA of 4 warps owns a
+// 128 x 64 tile of C, accumulated in tensor memory (TMEM, 64 FP32 columns x 128
+// lanes).  Per 16-wide k step every thread converts one row of A (threads 0-127) and
+// half a row of B (two threads per column) from FP32 to BF16 and stores them in the
+// no-swizzle K-major layout of the tensor core's shared-memory descriptors: 8 x 8
+// core matrices of 128 bytes, the two k halves 128 bytes apart (leading offset) and
+// consecutive groups of 8 rows 256 bytes apart (stride offset).  One elected thread
+// issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128, N = 64, K = 16) and
+// commits it to the stage's mbarrier; the staging of the next k step overlaps the
+// running MMA (two stages).  The epilogue reads the accumulator with tcgen05.ld (warp w
+// owns TMEM lanes 32w .. 32w + 31, i.e. tile rows), adds bias / ReLU or stores a
+// split-K plane exactly as k_gemm_bf16 does.  Every mbarrier wait is bounded: after
+// kTcSpin clock cycles the kernel records kTcTimeout in *err, issues no further MMA,
+// drains what it issued (again bounded) and frees its TMEM before returning.
+constexpr int kTcM = 128, kTcN = 64, kTcK = 16;
+constexpr uint32_t kTcCols = 64;            // TMEM columns: the FP32 accumulator of a 128 x 64 tile
+constexpr int kTcStages = 2;
+constexpr long long kTcSpin = 1LL << 31;    // SM clock cycles (about 1 s) before an mbarrier wait gives up
+constexpr int kTcTimeout = 1;
+// Dynamic shared memory per CTA.  At most 8 CTAs then fit on an SM (228 KB), so their
+// TMEM columns (8 x 64) never exceed the SM's 512 and tcgen05.alloc never waits.
+constexpr int kTcSmemBytes = 26 * 1024;
+
+struct __align__(1024) TcSmem {
+  uint4 a[kTcStages][kTcM * kTcK * 2 / 16];   // 128 rows x 16 k BF16 (4 KB) per stage
+  uint4 b[kTcStages][kTcN * kTcK * 2 / 16];   // 64 columns x 16 k BF16 (2 KB) per stage
+  unsigned long long bar[kTcStages];
+  uint32_t tmem;
+  int failed;
+};
+static_assert(sizeof(TcSmem) <= kTcSmemBytes, "tcgen05 GEMM shared memory");
+
+// Byte offset of row r (M or N index), k half g of a stage (no-swizzle K-major core matrices).
+__device__ __forceinline__ int tc_off(int r, int g) { return (r >> 3) * 256 + g * 128 + (r & 7) * 16; }
+
+// Shared-memory matrix descriptor: start address, leading (k) and stride (row-group)
+// byte offsets, each >> 4; bit 46 = descriptor version 1; layout type 0 = no swizzle.
+__device__ __forceinline__ uint64_t tc_desc(const void *p) {
+  uint64_t d = (uint64_t)((smem_addr(p) >> 4) & 0x3FFFu);
+  d |= (uint64_t)(128u >> 4) << 16;
+  d |= (uint64_t)(256u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                              ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void tc_bar_init(unsigned long long *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Waits for phase `parity` of the barrier (non-blocking polls); false once kTcSpin SM
+// clock cycles (about a second) have passed.
+__device__ __forceinline__ bool tc_bar_wait(unsigned long long *bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > kTcSpin) return false;
+  }
+}
+
+template <bool RELU, bool PARTIAL>
+__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, int kc, const float *__restrict__ A,
+                                                 long long sam, long long sak, const float *__restrict__ B,
+                                                 long long sbk, long long sbn, const float *__restrict__ bias,
+                                                 float *__restrict__ C, long long ldc, int *err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+  TcSmem &sm = *reinterpret_cast<TcSmem *>(tc_smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&sm.tmem)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int st = 0; st < kTcStages; st++) tc_bar_init(&sm.bar[st]);
+    sm.failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = sm.tmem;
+  const int steps = ke > kb ? (ke - kb + kTcK - 1) / kTcK : 0;
+  int issued = 0;
+  for (int it = 0; it < steps; it++) {
+    const int st = it & 1, k0 = kb + it * kTcK;
+    // the MMA that read this stage two steps ago must be done before it is overwritten
+    if (it >= kTcStages && !tc_bar_wait(&sm.bar[st], (uint32_t)(((it - kTcStages) >> 1) & 1))) sm.failed = 1;
+    __syncthreads();
+    if (sm.failed) break;
+    {
+      // A: thread t converts row m0 + t, k0 .. k0 + 15
+      const int m = m0 + tid;
+      uint32_t wv[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int k = k0 + 2 * q;
+        float x0 = 0.f, x1 = 0.f;
+        if (m < M) {
+          if (k < ke) x0 = A[m * sam + k * sak];
+          if (k + 1 < ke) x1 = A[m * sam + (k + 1) * sak];
+        }
+        wv[q] = bf16x2(x0, x1);
+      }
+      unsigned char *ab = reinterpret_cast<unsigned char *>(sm.a[st]);
+      *reinterpret_cast<uint4 *>(ab + tc_off(tid, 0)) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+      *reinterpret_cast<uint4 *>(ab + tc_off(tid, 1)) = make_uint4(wv[4], wv[5], wv[6], wv[7]);
+      // B: column n0 + (t & 63), k half t >> 6
+      const int nn = tid & 63, g = tid >> 6, n = n0 + nn;
+      uint32_t wb[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int k = k0 + 8 * g + 2 * q;
+        float y0 = 0.f, y1 = 0.f;
+        if (n < N) {
+          if (k < ke) y0 = B[k * sbk + n * sbn];
+          if (k + 1 < ke) y1 = B[(k + 1) * sbk + n * sbn];
+        }
+        wb[q] = bf16x2(y0, y1);
+      }
+      unsigned char *bb = reinterpret_cast<unsigned char *>(sm.b[st]);
+      *reinterpret_cast<uint4 *>(bb + tc_off(nn, g)) = make_uint4(wb[0], wb[1], wb[2], wb[3]);
+    }
+    // generic-proxy stores -> visible to the tensor core's (async proxy) reads
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint64_t da = tc_desc(sm.a[st]), db = tc_desc(sm.b[st]);
+      const uint32_t acc = it > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\t"
+          "setp.ne.b32 p, %4, 0;\n\t"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+          "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+          : "memory");
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_addr(&sm.bar[st]))
+                   : "memory");
+    }
+    issued = it + 1;
+  }
+  // every issued MMA has completed once the last one's commit arrived (one thread
+  // issues them all, in order)
+  bool ok = !sm.failed;
+  if (ok && issued > 0 && !tc_bar_wait(&sm.bar[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1))) ok = false;
+  if (!ok && issued > 0) tc_bar_wait(&sm.bar[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));   // drain
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok && tid == 0) atomicOr(err, kTcTimeout);
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (ok) {
+    const int row = m0 + 32 * w + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < kTcN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15}, [%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(ta)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+          const int col = n0 + c0 + e;
+          if (col >= N) continue;
+          float v = issued > 0 ? __uint_as_float(r[e]) : 0.f;
+          if (PARTIAL) {
+            C[((size_t)blockIdx.z * M + row) * N + col] = v;
+          } else {
+            if (bias) v += bias[col];
+            if (RELU) v = fmaxf(v, 0.f);
+            C[row * ldc + col] = v;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (w == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols) : "memory");
+  }
+}
+
 // ------------------------------------------------------------ batch input
 // Mean of each slot's points (before its transform), FP64 in a fixed tree order.
 __global__ void __launch_bounds__(256) k_slot_mean(const NetSlot *slots, float *mean, float *cent) {
@@ -414,6 +621,8 @@ struct NetDev {
   float *part = nullptr;                 // split-K and column-sum partials of the backward pass
   size_t part_cap = 0;
   int *arg = nullptr, *best = nullptr;
+  int gemm_kind = 0;                     // 0: tcgen05 (TMEM accumulators), 1: mma.sync (the second opinion)
+  int *err = nullptr;                    // device word: bounded waits that gave up (kTcTimeout)
 };
 
 size_t net_num_params() { return kNetParams; }
@@ -481,11 +690,28 @@ static int gemm_splits(long long K, int splits) {
 // C = A B (+bias, ReLU) on the tensor cores; with splits > 1 the k range is split over
 // blockIdx.z, the partial tiles go to part (gemm_splits(K, splits) M N floats) and are
 // added in a fixed order.
-static void gemm(Handle *h, bool relu, int M, int N, int K, const float *A, long long sam, long long sak,
-                 const float *B, long long sbk, long long sbn, const float *bias, float *C, long long ldc,
-                 int splits = 1, float *part = nullptr) {
+static void gemm(Handle *h, const NetDev *net, bool relu, int M, int N, int K, const float *A, long long sam,
+                 long long sak, const float *B, long long sbk, long long sbn, const float *bias, float *C,
+                 long long ldc, int splits = 1, float *part = nullptr) {
   const int kc = ((K + splits - 1) / splits + 15) / 16 * 16;
   splits = (K + kc - 1) / kc;
+  if (net->gemm_kind == 0) {
+    const dim3 tgrid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM, splits);
+    if (splits > 1) {
+      k_gemm_tc<false, true><<<tgrid, 128, kTcSmemBytes, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn,
+                                                                      nullptr, part, N, net->err);
+      k_split_sum<<<(unsigned)(((long long)M * N + 31) / 32), 256, 0, h->stream>>>(M, N, splits, part, C, ldc);
+      h->launches++;
+    } else if (relu) {
+      k_gemm_tc<true, false><<<tgrid, 128, kTcSmemBytes, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, bias,
+                                                                      C, ldc, net->err);
+    } else {
+      k_gemm_tc<false, false><<<tgrid, 128, kTcSmemBytes, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, bias,
+                                                                       C, ldc, net->err);
+    }
+    h->launches++;
+    return;
+  }
   const dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, splits);
   if (splits > 1) {
     k_gemm_bf16<false, true><<<grid, 128, 0, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, nullptr, part, N);
@@ -518,7 +744,8 @@ int net_create(Handle *h, int P, unsigned seed, NetDev **out) {
   if (cudaMalloc((void **)&n->w, sizeof(float) * np) != cudaSuccess ||
       cudaMalloc((void **)&n->g, sizeof(float) * np) != cudaSuccess ||
       cudaMalloc((void **)&n->m, sizeof(float) * np) != cudaSuccess ||
-      cudaMalloc((void **)&n->v, sizeof(float) * np) != cudaSuccess) {
+      cudaMalloc((void **)&n->v, sizeof(float) * np) != cudaSuccess ||
+      cudaMalloc((void **)&n->err, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     net_destroy(n);
     return CVO_ERR_OUT_OF_MEMORY;
@@ -543,7 +770,7 @@ int net_create(Handle *h, int P, unsigned seed, NetDev **out) {
   int rc = CVO_OK;
   if (cudaMemcpy(n->w, w.data(), sizeof(float) * np, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(n->g, 0, sizeof(float) * np) != cudaSuccess || cudaMemset(n->m, 0, sizeof(float) * np) != cudaSuccess ||
-      cudaMemset(n->v, 0, sizeof(float) * np) != cudaSuccess)
+      cudaMemset(n->v, 0, sizeof(float) * np) != cudaSuccess || cudaMemset(n->err, 0, sizeof(int)) != cudaSuccess)
     rc = set_cuda_error(h, cudaGetLastError(), "proposal network upload");
   if (rc) {
     net_destroy(n);
@@ -560,7 +787,26 @@ void net_destroy(NetDev *n) {
   cudaFree(n->g);
   cudaFree(n->m);
   cudaFree(n->v);
+  cudaFree(n->err);
   delete n;
+}
+
+// Reads (and clears) the network's device error word after the stream is synchronised:
+// a tensor-core GEMM whose bounded wait gave up reports CVO_ERR_TIMEOUT.
+static int net_check(Handle *h, NetDev *n) {
+  int e = 0;
+  CVO_CUDA_TRY(h, cudaMemcpyAsync(&e, n->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (!e) return CVO_OK;
+  CVO_CUDA_TRY(h, cudaMemsetAsync(n->err, 0, sizeof(int), h->stream));
+  h->last_error = "proposal network: a tensor-core GEMM gave up waiting for its MMAs";
+  return CVO_ERR_TIMEOUT;
+}
+
+int net_set_gemm(NetDev *n, int kind) {
+  if (kind != 0 && kind != 1) return CVO_ERR_INVALID_ARG;
+  n->gemm_kind = kind;
+  return CVO_OK;
 }
 
 int net_points(const NetDev *n) { return n->P; }
@@ -577,13 +823,13 @@ static int net_forward(Handle *h, NetDev *n, int Bn, const std::vector<NetSlot> 
   k_slot_mean<<<S, 256, 0, h->stream>>>(n->slots, n->mean, n->cent);
   k_net_inputs<<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(S, P, seed, n->slots, n->mean, n->X);
   h->launches += 2;
-  gemm(h, true, (int)rows, kNetH1, kNetIn, n->X, kNetIn, 1, n->w + kOffW1, kNetH1, 1, n->w + kOffB1, n->H1, kNetH1);
-  gemm(h, true, (int)rows, kNetH2, kNetH1, n->H1, kNetH1, 1, n->w + kOffW2, kNetH2, 1, n->w + kOffB2, n->H2, kNetH2);
+  gemm(h, n, true, (int)rows, kNetH1, kNetIn, n->X, kNetIn, 1, n->w + kOffW1, kNetH1, 1, n->w + kOffB1, n->H1, kNetH1);
+  gemm(h, n, true, (int)rows, kNetH2, kNetH1, n->H1, kNetH1, 1, n->w + kOffW2, kNetH2, 1, n->w + kOffB2, n->H2, kNetH2);
   k_maxpool<<<(S * kNetH2 + 255) / 256, 256, 0, h->stream>>>(S, P, n->H2, n->G, n->arg);
   h->launches++;
   // [e_src, e_tgt] of pair b is row b of G viewed as Bn x 256
-  gemm(h, true, Bn, kNetH3, kNetHead, n->G, kNetHead, 1, n->w + kOffW3, kNetH3, 1, n->w + kOffB3, n->H3, kNetH3);
-  gemm(h, false, Bn, kNetOut, kNetH3, n->H3, kNetH3, 1, n->w + kOffW4, kNetOut, 1, n->w + kOffB4, n->O, kNetOut);
+  gemm(h, n, true, Bn, kNetH3, kNetHead, n->G, kNetHead, 1, n->w + kOffW3, kNetH3, 1, n->w + kOffB3, n->H3, kNetH3);
+  gemm(h, n, false, Bn, kNetOut, kNetH3, n->H3, kNetH3, 1, n->w + kOffW4, kNetOut, 1, n->w + kOffB4, n->O, kNetOut);
   CVO_CUDA_TRY(h, cudaGetLastError());
   return CVO_OK;
 }
@@ -616,8 +862,7 @@ static int hypotheses_out(Handle *h, NetDev *n, int Bn, float *raw_out, float *T
   if (T_out)
     CVO_CUDA_TRY(h, cudaMemcpyAsync(T_out, n->Tout, sizeof(float) * Bn * kNetK * 16, cudaMemcpyDeviceToHost,
                                     h->stream));
-  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-  return CVO_OK;
+  return net_check(h, n);
 }
 
 // Forward over pool scenes (device arrays n_scenes x n_pts x 8: xyz + 5 features),
@@ -703,23 +948,23 @@ int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *s
   k_wta_loss<<<(Bn + 127) / 128, 128, 0, h->stream>>>(Bn, n->O, n->slots, n->cent, n->dO, n->loss, n->best);
   h->launches++;
   // head: O = H3 W4 + b4, H3 = relu(G' W3 + b3) with G' = G as Bn x 256
-  gemm(h, false, kNetH3, kNetOut, Bn, n->H3, 1, kNetH3, n->dO, kNetOut, 1, nullptr, g + kOffW4, kNetOut, 2, part);
+  gemm(h, n, false, kNetH3, kNetOut, Bn, n->H3, 1, kNetH3, n->dO, kNetOut, 1, nullptr, g + kOffW4, kNetOut, 2, part);
   colsum(h, Bn, kNetOut, n->dO, g + kOffB4, part);
-  gemm(h, false, Bn, kNetH3, kNetOut, n->dO, kNetOut, 1, w + kOffW4, 1, kNetOut, nullptr, n->dH3, kNetH3);
+  gemm(h, n, false, Bn, kNetH3, kNetOut, n->dO, kNetOut, 1, w + kOffW4, 1, kNetOut, nullptr, n->dH3, kNetH3);
   k_relu_bwd<<<(unsigned)(((long long)Bn * kNetH3 + 255) / 256), 256, 0, h->stream>>>((long long)Bn * kNetH3, n->H3,
                                                                                       n->dH3);
-  gemm(h, false, kNetHead, kNetH3, Bn, n->G, 1, kNetHead, n->dH3, kNetH3, 1, nullptr, g + kOffW3, kNetH3, 2, part);
+  gemm(h, n, false, kNetHead, kNetH3, Bn, n->G, 1, kNetHead, n->dH3, kNetH3, 1, nullptr, g + kOffW3, kNetH3, 2, part);
   colsum(h, Bn, kNetH3, n->dH3, g + kOffB3, part);
-  gemm(h, false, Bn, kNetHead, kNetH3, n->dH3, kNetH3, 1, w + kOffW3, 1, kNetH3, nullptr, n->dG, kNetHead);
+  gemm(h, n, false, Bn, kNetHead, kNetH3, n->dH3, kNetH3, 1, w + kOffW3, 1, kNetH3, nullptr, n->dG, kNetHead);
   // encoder: the max-pool routes dG to the pooled rows, then two ReLU layers
   CVO_CUDA_TRY(h, cudaMemsetAsync(n->dH2, 0, sizeof(float) * rows * kNetH2, h->stream));
   k_maxpool_bwd<<<(S * kNetH2 + 255) / 256, 256, 0, h->stream>>>(S, P, n->G, n->dG, n->arg, n->dH2);
-  gemm(h, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2, sp2,
+  gemm(h, n, false, kNetH1, kNetH2, (int)rows, n->H1, 1, kNetH1, n->dH2, kNetH2, 1, nullptr, g + kOffW2, kNetH2, sp2,
        part);
   colsum(h, (int)rows, kNetH2, n->dH2, g + kOffB2, part);
-  gemm(h, false, (int)rows, kNetH1, kNetH2, n->dH2, kNetH2, 1, w + kOffW2, 1, kNetH2, nullptr, n->dH1, kNetH1);
+  gemm(h, n, false, (int)rows, kNetH1, kNetH2, n->dH2, kNetH2, 1, w + kOffW2, 1, kNetH2, nullptr, n->dH1, kNetH1);
   k_relu_bwd<<<(unsigned)((rows * kNetH1 + 255) / 256), 256, 0, h->stream>>>(rows * kNetH1, n->H1, n->dH1);
-  gemm(h, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1, sp1,
+  gemm(h, n, false, kNetIn, kNetH1, (int)rows, n->X, 1, kNetIn, n->dH1, kNetH1, 1, nullptr, g + kOffW1, kNetH1, sp1,
        part);
   colsum(h, (int)rows, kNetH1, n->dH1, g + kOffB1, part);
   h->launches += 3;
@@ -733,7 +978,7 @@ int net_train_pool(Handle *h, NetDev *n, int n_scenes, int n_pts, const float *s
   CVO_CUDA_TRY(h, cudaGetLastError());
   std::vector<float> lh(Bn);
   CVO_CUDA_TRY(h, cudaMemcpyAsync(lh.data(), n->loss, sizeof(float) * Bn, cudaMemcpyDeviceToHost, h->stream));
-  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (int rc_err = net_check(h, n)) return rc_err;
   if (loss_out) {
     double s = 0.0;
     for (float x : lh) s += x;

@@ -109,6 +109,11 @@ class ProposalNet:
         L.check(L.lib().cvo_proposal_set(self._cvo._h, self._p, w.ctypes.data_as(_FP)), "cvo_proposal_set",
                 self._cvo._h)
 
+    def set_gemm(self, kind: int) -> None:
+        """Kernel of the matrix products: 0 the tcgen05 tensor-core GEMM (default), 1 the
+        mma.sync GEMM (a second opinion for tests)."""
+        L.check(L.lib().cvo_proposal_set_gemm(self._p, int(kind)), "cvo_proposal_set_gemm")
+
     def save(self, path: str) -> None:
         np.save(path, self.weights())
 

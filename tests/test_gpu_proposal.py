@@ -203,3 +203,26 @@ def test_cpu_pipeline_hypotheses_equal_device(cvo):
     H_cpu = cl.hypotheses(src, tgt)
     assert np.allclose(H_dev[:, :3, :3], H_cpu[:, :3, :3], atol=1e-4)
     assert np.allclose(H_dev[:, :3, 3], H_cpu[:, :3, 3], atol=1e-3 * (1 + np.abs(H_cpu[:, :3, 3]).max()))
+
+
+def test_tcgen05_gemm_matches_mma_sync(cvo, small_pool):
+    """The network's matrix products on the tcgen05 tensor cores (TMEM accumulators,
+    the default) against the warp-level mma.sync kernel kept as a second opinion:
+    both round the same FP32 operands to BF16 and accumulate in FP32, so outputs,
+    loss and gradients agree to accumulation order."""
+    rng = np.random.default_rng(21)
+    scene, T = _batch(rng, 7)
+    res = {}
+    for kind in (1, 0):
+        net = ProposalNet(cvo, points_per_cloud=P_SMALL, seed=9)
+        net.set_gemm(kind)
+        raw, hyp = net.forward_pool(small_pool, scene, T, seed=13)
+        loss = net.train_step(small_pool, scene, T, lr=0.0, seed=13)
+        res[kind] = (raw, hyp, loss, net.gradients())
+    raw1, hyp1, loss1, g1 = res[1]
+    raw0, hyp0, loss0, g0 = res[0]
+    scale = float(np.abs(raw1).max())
+    assert np.abs(raw0 - raw1).max() <= 1e-3 * scale
+    assert abs(loss0 - loss1) <= 1e-3 * abs(loss1)
+    assert np.linalg.norm(g0 - g1) <= 1e-2 * np.linalg.norm(g1)
+    assert np.allclose(hyp0[:, :, :3, :3], hyp1[:, :, :3, :3], atol=1e-3)
