@@ -556,11 +556,13 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) & ~(size_t)255; };
   int max_part_blocks = 0;
-  // spill-list entries per row (kept pairs beyond cap, row-major): up to kSelMax, at most 4 GB for the batch
+  // spill-list entries per row (kept pairs beyond cap, row-major): up to kSelMax, at most 16 GB for the
+  // batch (only the entries rows actually spill are ever written; a row that overflows its list is
+  // rescanned in index order, which costs far more than the memory)
   long long rows_all = 0;
   for (int p = 0; p < np; p++) rows_all += srcs[p]->n;
   int ov = kSelMax;
-  if (rows_all > 0) ov = (int)std::min<long long>(ov, (4ll << 30) / (8ll * rows_all));
+  if (rows_all > 0) ov = (int)std::min<long long>(ov, (16ll << 30) / (8ll * rows_all));
   ov &= ~3;   // spill rows start 16-byte aligned (k_select reads them with 16-byte loads)
   bh->ov = ov;
   const int ell_ld = (std::max(capmax, 1) + 3) & ~3;   // 16-byte aligned ELL rows

@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(BatchDev B, KParams K) 
 }
 
 // ------------------------------------------------------------ selection
-constexpr int kSelMax = 2048;      // kept pairs beyond cap one spill list can hold
+constexpr int kSelMax = 4096;      // kept pairs beyond cap one spill list can hold
 constexpr int kSelStage = 1024;    // rows up to this many entries are selected from shared memory
 constexpr int kSelThreads = 128;
 
