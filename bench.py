@@ -790,6 +790,7 @@ def run_component(args):
         cvo = CvoGPU(params=CvoParams(params_path("color")))
         pool = ScenePool(*ScenePool.generate(64, 2048, seed0=1_000_000))
         net = ProposalNet(cvo, points_per_cloud=512, seed=0)
+        net.set_gemm(1 if args.gemm == "mma" else 0)
         B, P = 64, 512
         rng = np.random.default_rng(0)
         batches = [(rng.integers(0, pool.n_scenes, size=B), np.stack([scenes.random_motion(rng) for _ in range(B)]),
@@ -826,7 +827,8 @@ def run_component(args):
                     "roofline": {"bound": "tensor", "achieved": round(tflops, 3), "peak": peak, "unit": "TFLOP/s",
                                  "frac": round(tflops / peak, 6) if peak else None,
                                  "note": "kernel launches and host synchronisation dominate: each product is small"},
-                    "config": {"batch": B, "points_per_cloud": P, "pool_scenes": 64}})
+                    "config": {"batch": B, "points_per_cloud": P, "pool_scenes": 64,
+                               "gemm": "tcgen05 (TMEM accumulators)" if args.gemm != "mma" else "mma.sync"}})
     print(json.dumps(out))
 
 
@@ -912,6 +914,8 @@ def main():
     ap.add_argument("--max-iter", type=int, default=0, help="override MAX_ITER (profiling runs only)")
     ap.add_argument("--eval-pairs", type=int, default=200, help="held-out pairs of --component global-eval")
     ap.add_argument("--eval-seed0", type=int, default=5000, help="first seed of --component global-eval's pairs")
+    ap.add_argument("--gemm", default="tcgen05", choices=["tcgen05", "mma"],
+                    help="matrix-product kernel of --component proposal")
     ap.add_argument("--component", default="",
                     choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval", "batching"],
                     help="time one component instead of the main workload")

@@ -190,37 +190,43 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, int kc, 
 // ------------------------------------------------------- tcgen05 GEMM
 // The same product on the fifth-generation tensor cores: one CTA of 4 warps owns a
 // 128 x 64 tile of C, accumulated in tensor memory (TMEM, 64 FP32 columns x 128
-// lanes).  Per 16-wide k step every thread converts one row of A (threads 0-127) and
-// half a row of B (two threads per column) from FP32 to BF16 and stores them in the
-// no-swizzle K-major layout of the tensor core's shared-memory descriptors: 8 x 8
-// core matrices of 128 bytes, the two k halves 128 bytes apart (leading offset) and
-// consecutive groups of 8 rows 256 bytes apart (stride offset).  One elected thread
-// issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128, N = 64, K = 16) and
-// commits it to the stage's mbarrier; the staging of the next k step overlaps the
-// running MMA (two stages).  The epilogue reads the accumulator with tcgen05.ld (warp w
-// owns TMEM lanes 32w .. 32w + 31, i.e. tile rows), adds bias / ReLU or stores a
-// split-K plane exactly as k_gemm_bf16 does.  Every mbarrier wait is bounded: after
-// kTcSpin clock cycles the kernel records kTcTimeout in *err, issues no further MMA,
-// drains what it issued (again bounded) and frees its TMEM before returning.
-constexpr int kTcM = 128, kTcN = 64, kTcK = 16;
+// lanes).  The k range is consumed in stages of 64: every thread converts one row of A
+// (threads 0-127) and half of a column of B (two threads per column) from FP32 to BF16
+// -- with 16-byte loads where k is the contiguous dimension -- and stores them in the
+// no-swizzle K-major layout of the tensor core's shared-memory descriptors: per 16-wide
+// k slice, 8 x 8 core matrices of 128 bytes, the slice's two k halves 128 bytes apart
+// (leading offset) and consecutive groups of 8 rows 256 bytes apart (stride offset).
+// One elected thread issues the stage's four tcgen05.mma (kind::f16, BF16 x BF16 ->
+// FP32, M = 128, N = 64, K = 16 each) and commits them to the stage's mbarrier; the
+// staging of the next stage overlaps the running MMAs (two stages).  The epilogue
+// reads the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w .. 32w + 31, i.e.
+// tile rows) and adds bias / ReLU or stores a split-K plane exactly as k_gemm_bf16
+// does.  Every mbarrier wait is bounded: after kTcSpin clock cycles the kernel records
+// kTcTimeout in *err, issues no further MMA, drains what it issued (again bounded) and
+// frees its TMEM before returning.
+constexpr int kTcM = 128, kTcN = 64, kTcK = 16, kTcSlices = 4, kTcKS = kTcK * kTcSlices;
 constexpr uint32_t kTcCols = 64;            // TMEM columns: the FP32 accumulator of a 128 x 64 tile
 constexpr int kTcStages = 2;
 constexpr long long kTcSpin = 1LL << 31;    // SM clock cycles (about 1 s) before an mbarrier wait gives up
 constexpr int kTcTimeout = 1;
-// Dynamic shared memory per CTA.  At most 8 CTAs then fit on an SM (228 KB), so their
-// TMEM columns (8 x 64) never exceed the SM's 512 and tcgen05.alloc never waits.
-constexpr int kTcSmemBytes = 26 * 1024;
+constexpr int kTcSliceA = kTcM * kTcK * 2;  // bytes of one 16-wide k slice of A (4 KB)
+constexpr int kTcSliceB = kTcN * kTcK * 2;  // and of B (2 KB)
+// Dynamic shared memory per CTA: at most 4 CTAs fit on an SM (228 KB), so their TMEM
+// columns (4 x 64) never exceed the SM's 512 and tcgen05.alloc never waits.
+constexpr int kTcSmemBytes = 52 * 1024;
 
 struct __align__(1024) TcSmem {
-  uint4 a[kTcStages][kTcM * kTcK * 2 / 16];   // 128 rows x 16 k BF16 (4 KB) per stage
-  uint4 b[kTcStages][kTcN * kTcK * 2 / 16];   // 64 columns x 16 k BF16 (2 KB) per stage
+  uint4 a[kTcStages][kTcSlices * kTcSliceA / 16];   // 128 rows x 64 k BF16 (16 KB) per stage
+  uint4 b[kTcStages][kTcSlices * kTcSliceB / 16];   // 64 columns x 64 k BF16 (8 KB) per stage
   unsigned long long bar[kTcStages];
   uint32_t tmem;
   int failed;
 };
 static_assert(sizeof(TcSmem) <= kTcSmemBytes, "tcgen05 GEMM shared memory");
+static_assert(kTcSmemBytes * 5 > 228 * 1024, "at most 4 tcgen05 GEMM CTAs per SM");
 
-// Byte offset of row r (M or N index), k half g of a stage (no-swizzle K-major core matrices).
+// Byte offset of row r (M or N index), k half g inside one 16-wide slice (no-swizzle
+// K-major core matrices).
 __device__ __forceinline__ int tc_off(int r, int g) { return (r >> 3) * 256 + g * 128 + (r & 7) * 16; }
 
 // Shared-memory matrix descriptor: start address, leading (k) and stride (row-group)
@@ -261,12 +267,26 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned long long *bar, uint32_t pa
   }
 }
 
+// Four consecutive k values of an operand row starting at k (zero beyond ke): one
+// 16-byte load when all four are in range, element loads at the ragged end.
+__device__ __forceinline__ float4 tc_load4(const float *src, int k, int ke) {
+  if (k + 3 < ke) return __ldg(reinterpret_cast<const float4 *>(src));
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (k < ke) x.x = src[0];
+  if (k + 1 < ke) x.y = src[1];
+  if (k + 2 < ke) x.z = src[2];
+  return x;
+}
+
 template <bool RELU, bool PARTIAL>
 __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, int kc, const float *__restrict__ A,
                                                  long long sam, long long sak, const float *__restrict__ B,
                                                  long long sbk, long long sbn, const float *__restrict__ bias,
                                                  float *__restrict__ C, long long ldc, int *err) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+  // k contiguous in memory, rows 16-byte aligned: operands are read with 16-byte loads
+  const bool vec_a = sak == 1 && (sam & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  const bool vec_b = sbk == 1 && (sbn & 3) == 0 && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
   TcSmem &sm = *reinterpret_cast<TcSmem *>(tc_smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
@@ -286,46 +306,67 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, int kc, co
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = sm.tmem;
-  const int steps = ke > kb ? (ke - kb + kTcK - 1) / kTcK : 0;
+  const int steps = ke > kb ? (ke - kb + kTcKS - 1) / kTcKS : 0;
   int issued = 0;
   for (int it = 0; it < steps; it++) {
-    const int st = it & 1, k0 = kb + it * kTcK;
-    // the MMA that read this stage two steps ago must be done before it is overwritten
+    const int st = it & 1, k0 = kb + it * kTcKS;
+    const int nsl = min(kTcSlices, (ke - k0 + kTcK - 1) / kTcK);   // 16-wide slices holding data
+    // the MMAs that read this stage two steps ago must be done before it is overwritten
     if (it >= kTcStages && !tc_bar_wait(&sm.bar[st], (uint32_t)(((it - kTcStages) >> 1) & 1))) sm.failed = 1;
     __syncthreads();
     if (sm.failed) break;
-    {
-      // A: thread t converts row m0 + t, k0 .. k0 + 15
-      const int m = m0 + tid;
+    unsigned char *ab = reinterpret_cast<unsigned char *>(sm.a[st]);
+    unsigned char *bb = reinterpret_cast<unsigned char *>(sm.b[st]);
+    const int m = m0 + tid;
+    const int nn = tid & 63, g = tid >> 6, n = n0 + nn;
+    for (int sl = 0; sl < nsl; sl++) {
+      const int ks = k0 + kTcK * sl;
+      // A: thread t converts row m0 + t, ks .. ks + 15
       uint32_t wv[8];
+      if (vec_a) {
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const int k = k0 + 2 * q;
-        float x0 = 0.f, x1 = 0.f;
-        if (m < M) {
-          if (k < ke) x0 = A[m * sam + k * sak];
-          if (k + 1 < ke) x1 = A[m * sam + (k + 1) * sak];
+        for (int q = 0; q < 4; q++) {
+          const float4 x = m < M ? tc_load4(A + m * sam + ks + 4 * q, ks + 4 * q, ke) : make_float4(0.f, 0.f, 0.f, 0.f);
+          wv[2 * q] = bf16x2(x.x, x.y);
+          wv[2 * q + 1] = bf16x2(x.z, x.w);
         }
-        wv[q] = bf16x2(x0, x1);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int k = ks + 2 * q;
+          float x0 = 0.f, x1 = 0.f;
+          if (m < M) {
+            if (k < ke) x0 = A[m * sam + k * sak];
+            if (k + 1 < ke) x1 = A[m * sam + (k + 1) * sak];
+          }
+          wv[q] = bf16x2(x0, x1);
+        }
       }
-      unsigned char *ab = reinterpret_cast<unsigned char *>(sm.a[st]);
-      *reinterpret_cast<uint4 *>(ab + tc_off(tid, 0)) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-      *reinterpret_cast<uint4 *>(ab + tc_off(tid, 1)) = make_uint4(wv[4], wv[5], wv[6], wv[7]);
-      // B: column n0 + (t & 63), k half t >> 6
-      const int nn = tid & 63, g = tid >> 6, n = n0 + nn;
+      *reinterpret_cast<uint4 *>(ab + sl * kTcSliceA + tc_off(tid, 0)) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+      *reinterpret_cast<uint4 *>(ab + sl * kTcSliceA + tc_off(tid, 1)) = make_uint4(wv[4], wv[5], wv[6], wv[7]);
+      // B: column n0 + (t & 63), k half t >> 6 of the slice
       uint32_t wb[4];
+      const int kh = ks + 8 * g;
+      if (vec_b) {
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int k = k0 + 8 * g + 2 * q;
-        float y0 = 0.f, y1 = 0.f;
-        if (n < N) {
-          if (k < ke) y0 = B[k * sbk + n * sbn];
-          if (k + 1 < ke) y1 = B[(k + 1) * sbk + n * sbn];
+        for (int q = 0; q < 2; q++) {
+          const float4 y = n < N ? tc_load4(B + n * sbn + kh + 4 * q, kh + 4 * q, ke) : make_float4(0.f, 0.f, 0.f, 0.f);
+          wb[2 * q] = bf16x2(y.x, y.y);
+          wb[2 * q + 1] = bf16x2(y.z, y.w);
         }
-        wb[q] = bf16x2(y0, y1);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int k = kh + 2 * q;
+          float y0 = 0.f, y1 = 0.f;
+          if (n < N) {
+            if (k < ke) y0 = B[k * sbk + n * sbn];
+            if (k + 1 < ke) y1 = B[(k + 1) * sbk + n * sbn];
+          }
+          wb[q] = bf16x2(y0, y1);
+        }
       }
-      unsigned char *bb = reinterpret_cast<unsigned char *>(sm.b[st]);
-      *reinterpret_cast<uint4 *>(bb + tc_off(nn, g)) = make_uint4(wb[0], wb[1], wb[2], wb[3]);
+      *reinterpret_cast<uint4 *>(bb + sl * kTcSliceB + tc_off(nn, g)) = make_uint4(wb[0], wb[1], wb[2], wb[3]);
     }
     // generic-proxy stores -> visible to the tensor core's (async proxy) reads
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -333,21 +374,23 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, int kc, co
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint64_t da = tc_desc(sm.a[st]), db = tc_desc(sm.b[st]);
-      const uint32_t acc = it > 0 ? 1u : 0u;
-      asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "setp.ne.b32 p, %4, 0;\n\t"
-          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-          "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
-          : "memory");
+      for (int sl = 0; sl < nsl; sl++) {
+        const uint64_t da = tc_desc(ab + sl * kTcSliceA), db = tc_desc(bb + sl * kTcSliceB);
+        const uint32_t acc = (it > 0 || sl > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+            : "memory");
+      }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                        smem_addr(&sm.bar[st]))
                    : "memory");
     }
     issued = it + 1;
   }
-  // every issued MMA has completed once the last one's commit arrived (one thread
+  // every issued MMA has completed once the last stage's commit arrived (one thread
   // issues them all, in order)
   bool ok = !sm.failed;
   if (ok && issued > 0 && !tc_bar_wait(&sm.bar[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1))) ok = false;
@@ -696,6 +739,15 @@ static void gemm(Handle *h, const NetDev *net, bool relu, int M, int N, int K, c
   const int kc = ((K + splits - 1) / splits + 15) / 16 * 16;
   splits = (K + kc - 1) / kc;
   if (net->gemm_kind == 0) {
+    // opt in above the 48 KB default of dynamic shared memory, once per device
+    static unsigned long long set_mask = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && !(set_mask & (1ull << (dev & 63)))) {
+      cudaFuncSetAttribute(k_gemm_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+      cudaFuncSetAttribute(k_gemm_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+      cudaFuncSetAttribute(k_gemm_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+      set_mask |= 1ull << (dev & 63);
+    }
     const dim3 tgrid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM, splits);
     if (splits > 1) {
       k_gemm_tc<false, true><<<tgrid, 128, kTcSmemBytes, h->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn,
