@@ -268,8 +268,9 @@ def run_ours(args):
         hyp0 = net.hypotheses([gs[0]], [gt[0]])[0, 0]
         r = cvo.autotune(gs[0], gt[0], hyp0, ell=args.refine_ell if args.refine_ell > 0 else p.ell_init, reps=2)
         b = r["configs"][r["best"]]
-        tune = {"div_r": b[0], "div_ext": b[1], "ms": round(b[2], 3),
-                "default_ms": round(next(ms for a, e, ms in r["configs"] if (a, e) == (4.0, 8.0)), 3)}
+        tune = {"div_r": b[0], "div_ext": b[1], "blocks_per_sm": b[2] if b[2] > 0 else "occupancy",
+                "ms": round(b[3], 3), "configs": len(r["configs"]),
+                "default_ms": round(next(ms for a, e, bp, ms in r["configs"] if (a, e, bp) == (4.0, 8.0, 0)), 3)}
 
     for _ in range(args.warmup):
         register_learned(gs, gt)

@@ -302,8 +302,9 @@ int cvo_register_hypotheses_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud
 /* The association's grid cell size for search radius r and source tiles of diagonal
  * ext is max(r / div_r, (ext + 2 r) / div_ext).  cvo_autotune_dev times one
  * association pass of (src, tgt) at pose T and lengthscale ell (<= 0: ell_init) for
- * each candidate (div_r in {2, 3, 4, 6} x div_ext in {4, 8, 16}; median of reps) and
- * keeps the fastest for every later batch with the same (F, C, log2 rows) key.  The
+ * each candidate (div_r in {2, 3, 4, 6} x div_ext in {4, 8, 16}; median of reps), then
+ * the best of these with 1 to 3 resident blocks per SM, and keeps the fastest for every
+ * later batch with the same (F, C, log2 rows) key (the arrays list all 15 candidates).  The
  * kernel matrix does not depend on the choice (kept pairs are defined by index order);
  * only the candidate work per row does.  Arrays (max_configs entries, may be NULL)
  * receive every candidate and its time in ms; best its index.  No reference
@@ -315,6 +316,17 @@ int cvo_autotune_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, cons
  * CVO_ERR_INVALID_ARG and the defaults (4, 8) for a key that was never tuned. */
 int cvo_tune_set(cvo_handle *h, int F, int C, int64_t rows, float div_r, float div_ext);
 int cvo_tune_get(const cvo_handle *h, int F, int C, int64_t rows, float *div_r, float *div_ext);
+/* The same with the launch dimension: after the 12 cell sizes, cvo_autotune_launch_dev
+ * times the best one with 1, 2 and 3 resident association blocks per SM (0 = as many as
+ * the occupancy allows, the default) and keeps the fastest of all 15; blocks_per_sm
+ * receives each candidate's value.  Like the cell size, the choice changes no result.
+ * No reference counterpart (its block sizes are compile-time, CMakeLists.txt:473-558). */
+int cvo_autotune_launch_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell,
+                            int reps, int max_configs, int *n_configs, float *div_r, float *div_ext,
+                            int *blocks_per_sm, float *ms, int *best);
+int cvo_tune_set_launch(cvo_handle *h, int F, int C, int64_t rows, float div_r, float div_ext, int blocks_per_sm);
+int cvo_tune_get_launch(const cvo_handle *h, int F, int C, int64_t rows, float *div_r, float *div_ext,
+                        int *blocks_per_sm);
 
 /* ---------------------------------------------------- adaptive-ell CVO */
 /* AdaptiveCvoGPU::align(source, target, init_guess_transform, transform, seconds)

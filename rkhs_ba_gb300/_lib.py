@@ -102,6 +102,9 @@ SIGNATURES = {
     "cvo_register_hypotheses_dev": (_i, [_P, _P, _P, _i, _FP, _f, _FP, _IP, _FP, _DP]),
     "cvo_autotune_dev": (_i, [_P, _P, _P, _FP, _f, _i, _i, _IP, _FP, _FP, _FP, _IP]),
     "cvo_tune_set": (_i, [_P, _i, _i, C.c_int64, _f, _f]),
+    "cvo_autotune_launch_dev": (_i, [_P, _P, _P, _FP, _f, _i, _i, _IP, _FP, _FP, _IP, _FP, _IP]),
+    "cvo_tune_set_launch": (_i, [_P, _i, _i, C.c_int64, _f, _f, _i]),
+    "cvo_tune_get_launch": (_i, [_P, _i, _i, C.c_int64, _FP, _FP, _IP]),
     "cvo_tune_get": (_i, [_P, _i, _i, C.c_int64, _FP, _FP]),
     "cvo_align_adaptive": (_i, [_P, C.POINTER(CvoCloudC), C.POINTER(CvoCloudC), _FP, _FP, _DP, _IP]),
     "cvo_align_adaptive_dev": (_i, [_P, _P, _P, _FP, _FP, _DP, _IP, _DP, _i]),

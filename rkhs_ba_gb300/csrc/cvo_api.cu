@@ -1077,6 +1077,29 @@ extern "C" int cvo_register_hypotheses_dev(cvo_handle *H, cvo_gpu_cloud *src, cv
 }
 
 // ------------------------------------------------------------ autotuner
+extern "C" int cvo_autotune_launch_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16],
+                                       float ell, int reps, int max_configs, int *n_configs, float *div_r,
+                                       float *div_ext, int *blocks_per_sm, float *ms, int *best) try {
+  if (!H || !src || !tgt || !T || max_configs < 0) return CVO_ERR_INVALID_ARG;
+  if (!(ell > 0.f)) ell = H->h.params.ell_init;
+  std::vector<TuneConfig> cfg;
+  std::vector<float> t;
+  int bi = 0;
+  int rc = autotune_association(&H->h, src->d, tgt->d, T, ell, reps, &cfg, &t, &bi);
+  if (rc) return rc;
+  if (n_configs) *n_configs = (int)cfg.size();
+  for (int k = 0; k < (int)cfg.size() && k < max_configs; k++) {
+    if (div_r) div_r[k] = cfg[k].cell_div_r;
+    if (div_ext) div_ext[k] = cfg[k].cell_div_ext;
+    if (blocks_per_sm) blocks_per_sm[k] = cfg[k].blocks_per_sm;
+    if (ms) ms[k] = t[k];
+  }
+  if (best) *best = bi;
+  return CVO_OK;
+} catch (...) {
+  return status_from_exception();
+}
+
 extern "C" int cvo_autotune_dev(cvo_handle *H, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell,
                                 int reps, int max_configs, int *n_configs, float *div_r, float *div_ext, float *ms,
                                 int *best) try {
@@ -1106,6 +1129,34 @@ extern "C" int cvo_tune_set(cvo_handle *H, int F, int C, int64_t rows, float div
   c.cell_div_ext = div_ext;
   H->h.tuned[tune_key(F, C, rows)] = c;
   return CVO_OK;
+} catch (...) {
+  return status_from_exception();
+}
+
+extern "C" int cvo_tune_set_launch(cvo_handle *H, int F, int C, int64_t rows, float div_r, float div_ext,
+                                   int blocks_per_sm) try {
+  if (!H || F < 0 || C < 0 || rows < 0 || !(div_r > 0.f) || !(div_ext > 0.f) || blocks_per_sm < 0)
+    return CVO_ERR_INVALID_ARG;
+  TuneConfig c;
+  c.cell_div_r = div_r;
+  c.cell_div_ext = div_ext;
+  c.blocks_per_sm = blocks_per_sm;
+  H->h.tuned[tune_key(F, C, rows)] = c;
+  return CVO_OK;
+} catch (...) {
+  return status_from_exception();
+}
+
+extern "C" int cvo_tune_get_launch(const cvo_handle *H, int F, int C, int64_t rows, float *div_r, float *div_ext,
+                                   int *blocks_per_sm) try {
+  if (!H || !div_r || !div_ext || !blocks_per_sm) return CVO_ERR_INVALID_ARG;
+  TuneConfig c;
+  auto it = H->h.tuned.find(tune_key(F, C, rows));
+  if (it != H->h.tuned.end()) c = it->second;
+  *div_r = c.cell_div_r;
+  *div_ext = c.cell_div_ext;
+  *blocks_per_sm = c.blocks_per_sm;
+  return it != H->h.tuned.end() ? CVO_OK : CVO_ERR_INVALID_ARG;
 } catch (...) {
   return status_from_exception();
 }

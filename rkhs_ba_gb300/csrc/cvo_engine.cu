@@ -719,9 +719,10 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
     int fch = K.use_int ? (F + 3) / 4 : 0, lch = K.use_sem ? label_chunks(C) : 0;
     B.record_bytes = 16 + 16 * fch + 16 * lch + (K.use_gtype ? 8 : 0);
   }
-  // persistent association blocks: one wave of resident blocks (work items are taken from a counter)
-  bh->assoc_blocks = std::max(1, std::min(B.total_warps / kCtaWarps,
-                                          bh->assoc_per_sm * (h->num_sms > 0 ? h->num_sms : 152)));
+  // persistent association blocks: one wave of resident blocks (work items are taken from a counter),
+  // at most the tuned number per SM
+  const int per_sm = tc.blocks_per_sm > 0 ? std::min(tc.blocks_per_sm, bh->assoc_per_sm) : bh->assoc_per_sm;
+  bh->assoc_blocks = std::max(1, std::min(B.total_warps / kCtaWarps, per_sm * (h->num_sms > 0 ? h->num_sms : 152)));
   bh->xform_blocks = (B.total_targets + 255) / 256;
   bh->sel_blocks = std::max(1, std::min(h->num_sms > 0 ? 4 * h->num_sms : 608, (total_rows + 3) / 4));
   return 0;
@@ -974,7 +975,8 @@ int run_inner_product_pairs(Handle *h, const std::vector<DevCloud *> &srcs, cons
 int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell, int reps,
                          std::vector<TuneConfig> *configs, std::vector<float> *ms, int *best) {
   NvtxRange nvtx_range("autotune");
-  // candidates: cells of r/2 .. r/6 against the radius, tile-box terms of 4 .. 16 cells
+  // candidates: cells of r/2 .. r/6 against the radius, tile-box terms of 4 .. 16 cells,
+  // all with the occupancy's blocks per SM; then 1 .. 3 blocks per SM with the best cells
   const float div_r[] = {2.f, 3.f, 4.f, 6.f};
   const float div_ext[] = {4.f, 8.f, 16.f};
   configs->clear();
@@ -998,6 +1000,33 @@ int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[
     h->tune_force = &(*configs)[k];
     std::vector<double> asum;
     rc = run_inner_product_pairs(h, {src}, {tgt}, Tv, ell, cap, &asum);   // builds this configuration's levels
+    std::vector<float> t;
+    for (int r = 0; r < reps && !rc; r++) {
+      cudaEventRecord(e0, h->stream);
+      rc = run_inner_product_pairs(h, {src}, {tgt}, Tv, ell, cap, &asum);
+      cudaEventRecord(e1, h->stream);
+      cudaEventSynchronize(e1);
+      float dt = 0.f;
+      cudaEventElapsedTime(&dt, e0, e1);
+      t.push_back(dt);
+    }
+    if (!rc) {
+      std::sort(t.begin(), t.end());
+      (*ms)[k] = t[t.size() / 2];
+      if ((*ms)[k] < (*ms)[bi]) bi = (int)k;
+    }
+  }
+  // then the launch: resident blocks per SM for the fastest cell size (fewer blocks give
+  // each one more items, which can even out a pass whose items differ widely in cost)
+  const int per_sm_max = 4;
+  for (int bps = 1; bps < per_sm_max && !rc; bps++) {
+    TuneConfig c = (*configs)[bi];
+    c.blocks_per_sm = bps;
+    configs->push_back(c);
+    ms->push_back(INFINITY);
+    const size_t k = configs->size() - 1;
+    h->tune_force = &(*configs)[k];
+    std::vector<double> asum;
     std::vector<float> t;
     for (int r = 0; r < reps && !rc; r++) {
       cudaEventRecord(e0, h->stream);

@@ -186,11 +186,14 @@ struct Profile {
 };
 
 // Association tuning: grid cell size h = max(r / cell_div_r, (ext + 2 r) / cell_div_ext)
-// for search radius r and source tiles of diagonal ext.  Results do not depend on it
-// (the kept pairs are defined by index order), only the work per row does.
+// for search radius r and source tiles of diagonal ext, and the resident association
+// blocks per SM of the persistent launch (0: as many as the occupancy allows).  Results
+// do not depend on either (the kept pairs are defined by index order), only the work per
+// row and how the work items spread over the SMs do.
 struct TuneConfig {
   float cell_div_r = 4.f;
   float cell_div_ext = 8.f;
+  int blocks_per_sm = 0;
 };
 
 struct Handle {

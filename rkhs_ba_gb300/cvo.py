@@ -467,17 +467,22 @@ class CvoGPU:
 
     # -- autotuner -----------------------------------------------------
     def autotune(self, source: GpuCloud, target: GpuCloud, T=None, ell: float = 0.0, reps: int = 3) -> dict:
-        """Times the association's cell-size configurations on one pair and keeps the fastest
-        for later batches of the same (F, C, size) key.  Returns {"configs": [(div_r, div_ext,
-        ms), ...], "best": index}."""
+        """Times the association's cell-size configurations on one pair, then the best one
+        with 1-3 resident blocks per SM, and keeps the fastest for later batches of the same
+        (F, C, size) key.  Returns {"configs": [(div_r, div_ext, blocks_per_sm, ms), ...],
+        "best": index}; blocks_per_sm 0 = as many as the occupancy allows."""
         Ti = _m16(np.eye(4) if T is None else T)
         n = C.c_int()
-        dr, de, ms = np.zeros(16, np.float32), np.zeros(16, np.float32), np.zeros(16, np.float32)
+        dr, de, ms = np.zeros(32, np.float32), np.zeros(32, np.float32), np.zeros(32, np.float32)
+        bp = np.zeros(32, np.int32)
         best = C.c_int()
-        L.check(L.lib().cvo_autotune_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP), float(ell),
-                                         int(reps), 16, C.byref(n), dr.ctypes.data_as(_FP), de.ctypes.data_as(_FP),
-                                         ms.ctypes.data_as(_FP), C.byref(best)), "cvo_autotune_dev", self._h)
-        return {"configs": [(float(dr[k]), float(de[k]), float(ms[k])) for k in range(n.value)], "best": best.value}
+        L.check(L.lib().cvo_autotune_launch_dev(self._h, source.handle, target.handle, Ti.ctypes.data_as(_FP),
+                                                float(ell), int(reps), 32, C.byref(n), dr.ctypes.data_as(_FP),
+                                                de.ctypes.data_as(_FP), bp.ctypes.data_as(C.POINTER(C.c_int)),
+                                                ms.ctypes.data_as(_FP), C.byref(best)),
+                "cvo_autotune_launch_dev", self._h)
+        return {"configs": [(float(dr[k]), float(de[k]), int(bp[k]), float(ms[k])) for k in range(n.value)],
+                "best": best.value}
 
     def tune_set(self, F: int, Cn: int, rows: int, div_r: float, div_ext: float) -> None:
         L.check(L.lib().cvo_tune_set(self._h, F, Cn, rows, float(div_r), float(div_ext)), "cvo_tune_set", self._h)
@@ -487,6 +492,16 @@ class CvoGPU:
         a, b = C.c_float(), C.c_float()
         rc = L.lib().cvo_tune_get(self._h, F, Cn, rows, C.byref(a), C.byref(b))
         return a.value, b.value, rc == 0
+
+    def tune_set_launch(self, F: int, Cn: int, rows: int, div_r: float, div_ext: float, blocks_per_sm: int) -> None:
+        L.check(L.lib().cvo_tune_set_launch(self._h, F, Cn, rows, float(div_r), float(div_ext), int(blocks_per_sm)),
+                "cvo_tune_set_launch", self._h)
+
+    def tune_get_launch(self, F: int, Cn: int, rows: int):
+        """(div_r, div_ext, blocks_per_sm, tuned?) for a key."""
+        a, b, c = C.c_float(), C.c_float(), C.c_int()
+        rc = L.lib().cvo_tune_get_launch(self._h, F, Cn, rows, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value, rc == 0
 
     # -- multi-frame ----------------------------------------------------
     def align_multi(self, clouds, poses, hold_const, edges):

@@ -187,7 +187,7 @@ def main():
             return np.eye(4), 0, np.ones(len(Ts)), 0.1
 
         def autotune(self, s, t, T, ell=0.0, reps=3):
-            return {"configs": [(4.0, 8.0, 2.0), (6.0, 4.0, 1.9)], "best": 1}
+            return {"configs": [(4.0, 8.0, 0, 2.0), (6.0, 4.0, 0, 1.9), (6.0, 4.0, 2, 1.8)], "best": 2}
 
         def profile(self, on=True):
             pass

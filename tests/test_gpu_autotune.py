@@ -1,7 +1,8 @@
-"""The association autotuner (cvo_autotune_dev): every candidate cell-size configuration
-gives the same kernel matrix (identical columns per row, values within 1e-6 relative)
-and the same inner product (1e-5 relative: row sums may add in another order); the
-fastest configuration is kept for later batches of the same key."""
+"""The association autotuner (cvo_autotune_launch_dev): every candidate configuration --
+12 cell sizes, then 1-3 resident blocks per SM -- gives the same kernel matrix (identical
+columns per row, values within 1e-6 relative) and the same inner product (1e-5
+relative: row sums may add in another order); the fastest configuration is kept for
+later batches of the same key."""
 import numpy as np
 import pytest
 
@@ -18,14 +19,15 @@ def test_autotune_configurations_agree(cuda_device):
     T = np.linalg.inv(T_gt) @ scenes.make_T(scenes.rot_axis_angle([0, 1, 0], np.radians(1.0)), [0.05, 0, 0.1])
     res = cvo.autotune(gs, gt, T, reps=2)
     cfgs = res["configs"]
-    assert len(cfgs) == 12 and 0 <= res["best"] < 12
-    assert all(np.isfinite(ms) and ms > 0 for _, _, ms in cfgs)
+    assert len(cfgs) == 15 and 0 <= res["best"] < 15
+    assert all(np.isfinite(ms) and ms > 0 for _, _, _, ms in cfgs)
+    assert [bp for _, _, bp, _ in cfgs] == [0] * 12 + [1, 2, 3]
     F, Cn = s.features.shape[1], 0
-    a, b, tuned = cvo.tune_get(F, Cn, len(s.xyz))
-    assert tuned and (a, b) == cfgs[res["best"]][:2]
+    a, b, bp, tuned = cvo.tune_get_launch(F, Cn, len(s.xyz))
+    assert tuned and (a, b, bp) == cfgs[res["best"]][:3]
     ref_assoc, ref_ip = None, None
-    for div_r, div_ext, _ in cfgs:
-        cvo.tune_set(F, Cn, len(s.xyz), div_r, div_ext)
+    for div_r, div_ext, bps, _ in cfgs:
+        cvo.tune_set_launch(F, Cn, len(s.xyz), div_r, div_ext, bps)
         assoc = cvo.compute_association_gpu(s, t, T, p.ell_init)
         ip = cvo.inner_product_batch(gs, gt, [T], p.ell_init)[0]
         if ref_assoc is None:
