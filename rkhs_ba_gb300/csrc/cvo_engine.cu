@@ -382,6 +382,12 @@ struct Workspace {
   char *dev = nullptr;
   size_t dev_cap = 0;
   int *pinned = nullptr;
+  // the last align batch's instantiated graph of kChunk iterations, and the launch
+  // parameters it was captured with: a later batch with the same parameters (same
+  // shapes in the same workspace) relaunches it without capturing again
+  cudaGraphExec_t align_exec = nullptr;
+  std::vector<unsigned char> align_key;
+  long long align_per_chunk = 0;
 };
 
 static int ensure_workspace(Handle *h, size_t bytes) {
@@ -390,6 +396,8 @@ static int ensure_workspace(Handle *h, size_t bytes) {
   if (!w->pinned) CVO_CUDA_TRY(h, cudaMallocHost((void **)&w->pinned, 4096));
   if (w->dev_cap >= bytes) return 0;
   if (w->dev) { cudaStreamSynchronize(h->stream); cudaFree(w->dev); w->dev = nullptr; w->dev_cap = 0; }
+  // a cached graph's kernels point into the old workspace
+  if (w->align_exec) { cudaGraphExecDestroy(w->align_exec); w->align_exec = nullptr; w->align_key.clear(); }
   size_t want = bytes + bytes / 4 + (1 << 20);
   cudaError_t e = cudaMalloc((void **)&w->dev, want);
   if (e != cudaSuccess) {
@@ -402,6 +410,7 @@ static int ensure_workspace(Handle *h, size_t bytes) {
 
 void free_workspace(Handle *h) {
   if (!h->ws) return;
+  if (h->ws->align_exec) cudaGraphExecDestroy(h->ws->align_exec);
   if (h->ws->dev) cudaFree(h->ws->dev);
   if (h->ws->pinned) cudaFreeHost(h->ws->pinned);
   delete h->ws;
@@ -850,7 +859,9 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, h->stream);
-  // capture one chunk of iterations as a CUDA graph and relaunch it
+  // capture one chunk of iterations as a CUDA graph and relaunch it; without profiling
+  // events the instantiated graph is kept in the workspace and reused by a later batch
+  // whose launch parameters are byte-identical
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   long long before = h->launches;
@@ -858,16 +869,49 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
   // event-record nodes of the graph
   constexpr int kEv = 7;
   std::vector<cudaEvent_t> pev;
-  if (h->prof.on) {
-    pev.resize(kEv * kChunk);
-    for (auto &e : pev) cudaEventCreate(&e);
+  std::vector<unsigned char> key;
+  {
+    auto add = [&](const void *p, size_t n) {
+      const unsigned char *c = static_cast<const unsigned char *>(p);
+      key.insert(key.end(), c, c + n);
+    };
+    add(&bh.B, sizeof(bh.B));
+    add(&K, sizeof(K));
+    add(&bh.assoc, sizeof(bh.assoc));
+    add(&bh.rescan, sizeof(bh.rescan));
+    add(&bh.assoc_smem, sizeof(bh.assoc_smem));
+    add(&bh.assoc_blocks, sizeof(bh.assoc_blocks));
+    add(&bh.xform_blocks, sizeof(bh.xform_blocks));
+    add(&bh.sel_blocks, sizeof(bh.sel_blocks));
+    add(&bh.src_max_norm, sizeof(bh.src_max_norm));
+    add(&h->stream, sizeof(h->stream));
   }
-  CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int it = 0; it < kChunk; it++) launch_iteration(h, &bh, K, h->prof.on ? &pev[kEv * it] : nullptr);
-  CVO_CUDA_TRY(h, cudaStreamEndCapture(h->stream, &graph));
-  long long per_chunk = h->launches - before;
-  h->launches = before;
-  CVO_CUDA_TRY(h, cudaGraphInstantiate(&exec, graph, 0));
+  Workspace *ws = h->ws;
+  const bool reuse = !h->prof.on && ws->align_exec && ws->align_key == key;
+  long long per_chunk = 0;
+  if (reuse) {
+    exec = ws->align_exec;
+    per_chunk = ws->align_per_chunk;
+  } else {
+    if (h->prof.on) {
+      pev.resize(kEv * kChunk);
+      for (auto &e : pev) cudaEventCreate(&e);
+    }
+    CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < kChunk; it++) launch_iteration(h, &bh, K, h->prof.on ? &pev[kEv * it] : nullptr);
+    CVO_CUDA_TRY(h, cudaStreamEndCapture(h->stream, &graph));
+    per_chunk = h->launches - before;
+    h->launches = before;
+    CVO_CUDA_TRY(h, cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    graph = nullptr;
+    if (!h->prof.on) {
+      if (ws->align_exec) cudaGraphExecDestroy(ws->align_exec);
+      ws->align_exec = exec;
+      ws->align_key = key;
+      ws->align_per_chunk = per_chunk;
+    }
+  }
   int *active_h = h->ws->pinned;
   long long max_chunks = (long long)h->params.MAX_ITER / kChunk + 2;
   long long iters_seen = 0;
@@ -916,8 +960,7 @@ int run_align_batch(Handle *h, const std::vector<DevCloud *> &srcs, const std::v
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
+  if (exec != ws->align_exec) cudaGraphExecDestroy(exec);   // profiled graphs are not kept
   if (secs) *secs = ms / 1000.0;
   if ((rc = check_err(h, &bh))) return rc;
   if ((rc = read_pairs(h, &bh))) return rc;

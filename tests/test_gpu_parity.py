@@ -237,3 +237,28 @@ def test_reference_demo_clouds_match_oracle_fixture(cuda_device):
         assert ret == int(g[ret_key]) and iters == int(g[it_key])
         T_o = g[T_key]
         assert _rot_err(T, T_o) < tol and np.linalg.norm(T[:3, 3] - T_o[:3, 3]) < tol, max_iter
+
+
+def test_align_graph_reused_across_batches(cuda_device):
+    """A second batch with the same shapes relaunches the first batch's instantiated
+    CUDA graph: its results equal those of a fresh handle (which captures anew), for the
+    same pairs and for different pairs of the same sizes."""
+    p = CvoParams(params_path("geometric"))
+    p.MAX_ITER = 30
+    pairs = [scenes.room_pair(n=2500, seed=s) for s in (41, 42)]
+    other = [scenes.room_pair(n=2500, seed=s) for s in (43, 44)]
+    cvo = CvoGPU(params=p)
+    gs = [cvo.upload(a) for a, _, _ in pairs]
+    gt = [cvo.upload(b) for _, b, _ in pairs]
+    first = cvo.align_batch(gs, gt, [np.eye(4)] * 2)
+    again = cvo.align_batch(gs, gt, [np.eye(4)] * 2)
+    for k in range(2):
+        assert np.array_equal(first[0][k], again[0][k]) and first[2][k] == again[2][k]
+    os_ = [cvo.upload(a) for a, _, _ in other]
+    ot = [cvo.upload(b) for _, b, _ in other]
+    reused = cvo.align_batch(os_, ot, [np.eye(4)] * 2)
+    fresh_cvo = CvoGPU(params=p)
+    fresh = fresh_cvo.align_batch([fresh_cvo.upload(a) for a, _, _ in other],
+                                  [fresh_cvo.upload(b) for _, b, _ in other], [np.eye(4)] * 2)
+    for k in range(2):
+        assert np.array_equal(reused[0][k], fresh[0][k]) and reused[2][k] == fresh[2][k]
