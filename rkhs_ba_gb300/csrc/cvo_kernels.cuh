@@ -766,18 +766,23 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
 // of the selection touches global memory only to write the result.  A radix select
 // over d = j - jmin (jmin, jmax: the row's smallest and largest kept index; 9-bit
 // digits from the highest bit of jmax - jmin, warp-private histograms) finds the
-// cap-th smallest index r.  Offsetting by jmin spreads neighbouring indices over the
-// bins, so the histogram atomics rarely collide and a row whose indices span fewer
-// than 512 values needs one pass.  The entries with index <= r (exactly cap: indices
+// cap-th smallest index r.  Offsetting by jmin spreads the indices over the bins, each
+// lane counts its own run of the list (so one instruction's increments come from
+// different grid cells and rarely collide), and a row whose indices span fewer than 512
+// values needs one pass.  The entries with index <= r (exactly cap: indices
 // are distinct) are compacted in list order into the ELL slots.  Longer rows read
 // their entries from global memory on every pass; the compaction is then in place
 // (an entry is read before any write can reach its slot).
 constexpr int kSelBins = 512;
 constexpr int kSelDigit = 9;
+// bin b lives at b + b / 16: lane l's scan reads its 16 bins at stride 17 words, on
+// distinct banks
+constexpr int kSelHist = kSelBins + kSelBins / 16;
+__device__ __forceinline__ int sel_bin(int b) { return b + (b >> 4); }
 __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
   __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
   __shared__ float vbuf_all[kSelThreads / 32][kSelStage];
-  __shared__ int hist_all[kSelThreads / 32][kSelBins];
+  __shared__ int hist_all[kSelThreads / 32][kSelHist];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *jb = jbuf_all[w];
   float *vb = vbuf_all[w];
@@ -855,17 +860,25 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     int prefix = 0, target = cap;
     for (int hs = bits; hs > 0; hs -= kSelDigit) {
       const int sh = max(hs - kSelDigit, 0), wd = hs - sh;
-      for (int b = lane; b < kSelBins; b += 32) hist[b] = 0;
+      for (int b = lane; b < kSelHist; b += 32) hist[b] = 0;
       __syncwarp();
-      for (int t = lane; t < E; t += 32) {
-        const int d = entry(t) - jmin;
-        if ((d >> hs) == (prefix >> hs)) atomicAdd(&hist[(d >> sh) & ((1 << wd) - 1)], 1);
+      // lane l counts the contiguous run of entries l * per .. : neighbouring entries of
+      // the list come from one grid cell and share their high index bits, so the 32
+      // increments of one instruction then go to different bins instead of colliding (an
+      // odd run length keeps the 32 lanes' shared-memory reads on distinct banks)
+      const int per = ((E + 31) >> 5) | 1;
+      for (int i = 0; i < per; i++) {
+        const int t = lane * per + i;
+        if (t < E) {
+          const int d = entry(t) - jmin;
+          if ((d >> hs) == (prefix >> hs)) atomicAdd(&hist[sel_bin((d >> sh) & ((1 << wd) - 1))], 1);
+        }
       }
       __syncwarp();
       constexpr int kPer = kSelBins / 32;
       int loc = 0;
 #pragma unroll
-      for (int i = 0; i < kPer; i++) loc += hist[lane * kPer + i];
+      for (int i = 0; i < kPer; i++) loc += hist[sel_bin(lane * kPer + i)];
       int incl = loc;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -878,7 +891,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       int bin = L * kPer;
 #pragma unroll 1
       for (int i = 0; i < kPer; i++) {
-        const int hb = hist[L * kPer + i];
+        const int hb = hist[sel_bin(L * kPer + i)];
         if (run + hb >= target) { bin = L * kPer + i; break; }
         run += hb;
       }
