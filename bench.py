@@ -785,6 +785,31 @@ def run_component(args):
                     "legs": out_legs,
                     "config": {"pairs_points": sizes, "hypotheses_points": args.points, "params": "color.yaml",
                                "hypotheses": "24-rotation grid, one global pair", "timing": "host clock, synchronised"}})
+    elif args.component == "align":
+        # the refinement stage of the learned pipeline on its own: one batched align of
+        # --pairs global pairs, each started 5 deg / 10 cm from its ground truth, from
+        # ell = --refine-ell (the workload whose association kernel the profiles capture)
+        p = CvoParams(params_path("color"))
+        p.ell_init = args.refine_ell if args.refine_ell > 0 else p.ell_init
+        if args.max_iter > 0:
+            p.MAX_ITER = args.max_iter
+        cvo = CvoGPU(params=p)
+        pairs = make_pairs(args.pairs, args.points)
+        gs = [cvo.upload(s) for s, _, _ in pairs]
+        gt = [cvo.upload(t) for _, t, _ in pairs]
+        dT = scenes.make_T(scenes.rot_axis_angle([0.3, 1.0, 0.2], np.radians(5.0)), [0.1, 0.0, 0.0])
+        inits = [np.asarray(T_gt, np.float64) @ dT for _, _, T_gt in pairs]
+        res = {}
+
+        def run():
+            res["r"] = cvo.align_batch(gs, gt, inits)
+        sec = timed(run)
+        its = res["r"][2]
+        out.update({"metric": "batched refinement registrations/s (%d pairs x %d points)" % (args.pairs, args.points),
+                    "unit": "registrations/s", "value": round(args.pairs / sec, 4), "ms_per_call": round(sec * 1000, 3),
+                    "iterations": [int(i) for i in its],
+                    "config": {"pairs": args.pairs, "points_per_cloud": args.points, "params": "color.yaml",
+                               "ell_init": p.ell_init, "max_iter": p.MAX_ITER, "start": "ground truth x (5 deg, 10 cm)"}})
     elif args.component == "proposal":
         from oracle import proposal as op
         from rkhs_ba_gb300.proposal import ProposalNet, ScenePool
@@ -918,7 +943,8 @@ def main():
     ap.add_argument("--gemm", default="tcgen05", choices=["tcgen05", "mma"],
                     help="matrix-product kernel of --component proposal")
     ap.add_argument("--component", default="",
-                    choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval", "batching"],
+                    choices=["", "irls", "aniso", "frontend", "proposal", "adaptive", "global-eval", "batching",
+                             "align"],
                     help="time one component instead of the main workload")
     args = ap.parse_args()
     from rkhs_ba_gb300 import _build
