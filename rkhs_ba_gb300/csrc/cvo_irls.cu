@@ -53,7 +53,9 @@ struct IrlsEdge {
 };
 
 // Accumulates, per block, the cost and (WANT_J) the 12x12 J^T J and J^T r of the
-// residuals of one edge.  One thread per row; per-row sums in FP32, block sums in FP64.
+// residuals of one edge.  One thread per row; the row's point is moved with the FP64
+// poses once, every entry is then single precision (see the residual below); per-row
+// sums in FP32, block sums in FP64.
 template <bool WANT_J>
 __global__ void __launch_bounds__(kIrlsThreads) k_irls_accum(const IrlsEdge *E, int ne, const double *poses,
                                                               double *partial) {
@@ -74,31 +76,44 @@ __global__ void __launch_bounds__(kIrlsThreads) k_irls_accum(const IrlsEdge *E, 
     const double *T1 = poses + 12 * ed.f1, *T2 = poses + 12 * ed.f2;
     const int z = min(ed.nnz_row[s], ed.lim);
     const float4 a1 = ed.p1[s];
+    // The residual vector e = T1 p1 - T2 p2 (world frame) is a difference of two points
+    // tens of metres out that lie centimetres apart.  Per row, p1 is taken to the target
+    // frame in double, p1' = R2^T (T1 p1 - t2), and split into float hi + lo; per entry
+    // d = (hi - p2) + lo is then exact to float rounding of d itself (hi - p2 cancels
+    // without error for nearby points), e = R2 d, |e| = |d|, R2^T e = d and
+    // R1^T e = (R1^T R2) d.  So the per-entry arithmetic is single precision without the
+    // cancellation a float e = q1 - q2 would suffer.
     const double p1[3] = {a1.x, a1.y, a1.z};
-    double q1[3];
+    double q1[3], pd[3];
     for (int r = 0; r < 3; r++) q1[r] = T1[4 * r] * p1[0] + T1[4 * r + 1] * p1[1] + T1[4 * r + 2] * p1[2] + T1[4 * r + 3];
+    for (int r = 0; r < 3; r++)
+      pd[r] = T2[r] * (q1[0] - T2[3]) + T2[4 + r] * (q1[1] - T2[7]) + T2[8 + r] * (q1[2] - T2[11]);
+    float ph[3], pl[3], R12[9];
+    for (int r = 0; r < 3; r++) {
+      ph[r] = (float)pd[r];
+      pl[r] = (float)(pd[r] - (double)ph[r]);
+    }
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++)
+        R12[3 * r + c] = (float)(T1[r] * T2[c] + T1[4 + r] * T2[4 + c] + T1[8 + r] * T2[8 + c]);
+    float cost_f = 0.f;
     for (int c = 0; c < z; c++) {
       const int j = ed.A_j[(size_t)s * ed.ld + c];
-      const double a = ed.A_v[(size_t)s * ed.ld + c];
+      const float a = ed.A_v[(size_t)s * ed.ld + c];
       const float4 b2 = __ldg(&ed.p2[j]);
-      const double p2[3] = {b2.x, b2.y, b2.z};
-      double ev[3];
-      for (int r = 0; r < 3; r++)
-        ev[r] = q1[r] - (T2[4 * r] * p2[0] + T2[4 * r + 1] * p2[1] + T2[4 * r + 2] * p2[2] + T2[4 * r + 3]);
-      const double rr = a * (ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
-      cost += 0.5 * rr * rr;
+      const float d[3] = {(ph[0] - b2.x) + pl[0], (ph[1] - b2.y) + pl[1], (ph[2] - b2.z) + pl[2]};
+      const float rr = a * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      cost_f = fmaf(0.5f * rr, rr, cost_f);
       if (WANT_J) {
-        float u1[3], u2[3], J[12];
-        for (int r = 0; r < 3; r++) {
-          u1[r] = (float)(T1[r] * ev[0] + T1[4 + r] * ev[1] + T1[8 + r] * ev[2]);   // R1^T e
-          u2[r] = (float)(T2[r] * ev[0] + T2[4 + r] * ev[1] + T2[8 + r] * ev[2]);   // R2^T e
-        }
+        float u1[3], J[12];
+        const float *u2 = d;                                                        // R2^T e
+        for (int r = 0; r < 3; r++) u1[r] = R12[3 * r] * d[0] + R12[3 * r + 1] * d[1] + R12[3 * r + 2] * d[2];   // R1^T e
         const float x1 = a1.x, y1 = a1.y, z1 = a1.z, x2 = b2.x, y2 = b2.y, z2 = b2.z;
         J[0] = u1[0]; J[1] = u1[1]; J[2] = u1[2];
         J[3] = y1 * u1[2] - z1 * u1[1]; J[4] = z1 * u1[0] - x1 * u1[2]; J[5] = x1 * u1[1] - y1 * u1[0];
         J[6] = -u2[0]; J[7] = -u2[1]; J[8] = -u2[2];
         J[9] = -(y2 * u2[2] - z2 * u2[1]); J[10] = -(z2 * u2[0] - x2 * u2[2]); J[11] = -(x2 * u2[1] - y2 * u2[0]);
-        const float rf = (float)rr;
+        const float rf = rr;
         int k = 0;
 #pragma unroll
         for (int p = 0; p < 12; p++)
@@ -108,6 +123,7 @@ __global__ void __launch_bounds__(kIrlsThreads) k_irls_accum(const IrlsEdge *E, 
         for (int p = 0; p < 12; p++) acc[78 + p] = fmaf(J[p], rf, acc[78 + p]);
       }
     }
+    cost = (double)cost_f;
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (WANT_J) {
