@@ -269,6 +269,8 @@ def run_ours(args):
         r = cvo.autotune(gs[0], gt[0], hyp0, ell=args.refine_ell if args.refine_ell > 0 else p.ell_init, reps=2)
         b = r["configs"][r["best"]]
         tune = {"div_r": b[0], "div_ext": b[1], "blocks_per_sm": b[2] if b[2] > 0 else "occupancy",
+                "blocks_per_sm_applies_to": "batches with the tuned pair's work items (the 8-pair steps keep the "
+                                            "occupancy default)",
                 "ms": round(b[3], 3), "configs": len(r["configs"]),
                 "default_ms": round(next(ms for a, e, bp, ms in r["configs"] if (a, e, bp) == (4.0, 8.0, 0)), 3)}
 

@@ -320,6 +320,9 @@ int cvo_tune_get(const cvo_handle *h, int F, int C, int64_t rows, float *div_r, 
  * times the best one with 1, 2 and 3 resident association blocks per SM (0 = as many as
  * the occupancy allows, the default) and keeps the fastest of all 15; blocks_per_sm
  * receives each candidate's value.  Like the cell size, the choice changes no result.
+ * The cell size applies to later batches of pairs of the key's size; the blocks per SM
+ * only to batches with as many work items (128 source rows each) as the tuned pair, i.e.
+ * single-pair batches of that size (batches of many pairs keep the occupancy default).
  * No reference counterpart (its block sizes are compile-time, CMakeLists.txt:473-558). */
 int cvo_autotune_launch_dev(cvo_handle *h, cvo_gpu_cloud *src, cvo_gpu_cloud *tgt, const float T[16], float ell,
                             int reps, int max_configs, int *n_configs, float *div_r, float *div_ext,

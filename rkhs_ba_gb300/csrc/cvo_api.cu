@@ -1140,8 +1140,8 @@ extern "C" int cvo_tune_set_launch(cvo_handle *H, int F, int C, int64_t rows, fl
   TuneConfig c;
   c.cell_div_r = div_r;
   c.cell_div_ext = div_ext;
-  c.blocks_per_sm = blocks_per_sm;
   H->h.tuned[tune_key(F, C, rows)] = c;
+  H->h.tuned_bps[tune_key(F, C, tune_items(rows))] = blocks_per_sm;
   return CVO_OK;
 } catch (...) {
   return status_from_exception();
@@ -1155,7 +1155,8 @@ extern "C" int cvo_tune_get_launch(const cvo_handle *H, int F, int C, int64_t ro
   if (it != H->h.tuned.end()) c = it->second;
   *div_r = c.cell_div_r;
   *div_ext = c.cell_div_ext;
-  *blocks_per_sm = c.blocks_per_sm;
+  auto ib = H->h.tuned_bps.find(tune_key(F, C, tune_items(rows)));
+  *blocks_per_sm = ib != H->h.tuned_bps.end() ? ib->second : 0;
   return it != H->h.tuned.end() ? CVO_OK : CVO_ERR_INVALID_ARG;
 } catch (...) {
   return status_from_exception();

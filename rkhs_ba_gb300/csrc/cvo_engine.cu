@@ -479,6 +479,8 @@ static float radius_for_cell(float hc, float ext, const TuneConfig &c) {
   return std::max(0.f, std::min(c.cell_div_r * hc, 0.5f * (c.cell_div_ext * hc - ext)));
 }
 
+long long tune_items(long long rows) { return (rows + 32 * kCtaWarps - 1) / (32 * kCtaWarps); }
+
 long long tune_key(int F, int C, long long rows) {
   int b = 0;
   while ((1LL << (b + 1)) <= rows && b < 40) b++;
@@ -522,14 +524,23 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   int rc = select_kernels(K, F, C, bh->assoc, bh->rescan, bh->assoc_smem, bh->assoc_per_sm);
   if (rc) return rc;
   // cell-size configuration: forced by the autotuner, else the tuned one for this key, else the default
+  // The cell size is keyed by the pairs' size (it sets the work per row); the blocks per
+  // SM by the batch's number of work items (it sets how the items spread over the SMs),
+  // so a value tuned on one pair does not carry over to a batch of many.
   TuneConfig tc;
   if (h->tune_force) {
     tc = *h->tune_force;
   } else {
-    long long maxn = 0;
-    for (int p = 0; p < np; p++) maxn = std::max<long long>(maxn, srcs[p]->n);
+    long long maxn = 0, items = 0;
+    for (int p = 0; p < np; p++) {
+      maxn = std::max<long long>(maxn, srcs[p]->n);
+      items += (srcs[p]->n + 32 * kCtaWarps - 1) / (32 * kCtaWarps);
+    }
     auto it = h->tuned.find(tune_key(F, C, maxn));
     if (it != h->tuned.end()) tc = it->second;
+    tc.blocks_per_sm = 0;
+    auto ib = h->tuned_bps.find(tune_key(F, C, items));
+    if (ib != h->tuned_bps.end()) tc.blocks_per_sm = ib->second;
   }
   // grid levels per pair
   std::vector<std::vector<GridDesc>> lv(np);
@@ -1090,7 +1101,10 @@ int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
-  h->tuned[tune_key(src->F, src->C, src->n)] = (*configs)[bi];
+  TuneConfig cell = (*configs)[bi];
+  h->tuned_bps[tune_key(src->F, src->C, tune_items(src->n))] = cell.blocks_per_sm;
+  cell.blocks_per_sm = 0;
+  h->tuned[tune_key(src->F, src->C, src->n)] = cell;
   if (best) *best = bi;
   return CVO_OK;
 }

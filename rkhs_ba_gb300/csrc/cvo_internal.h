@@ -206,11 +206,14 @@ struct Handle {
   long long launches = 0;
   std::string last_error;
   Workspace *ws = nullptr;
-  std::map<long long, TuneConfig> tuned;    // (F, C, log2 rows) -> fastest configuration
+  std::map<long long, TuneConfig> tuned;    // (F, C, log2 rows) -> fastest cell size
+  std::map<long long, int> tuned_bps;       // (F, C, log2 work items of a batch) -> blocks per SM
   const TuneConfig *tune_force = nullptr;   // set while the autotuner times a configuration
 };
 
 long long tune_key(int F, int C, long long rows);
+// Association work items (128 source rows each) of a pair of `rows` source points.
+long long tune_items(long long rows);
 // Times one association pass of (src, tgt) at pose T and lengthscale ell for every
 // candidate configuration and records the fastest for the batches that match its key.
 int autotune_association(Handle *h, DevCloud *src, DevCloud *tgt, const float T[16], float ell, int reps,
