@@ -25,6 +25,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 METRICS = ("dram__bytes_read.sum", "dram__bytes_write.sum", "smsp__inst_executed.sum", "gpu__time_duration.sum")
 
 
+# unit strings of the raw page -> bytes or nanoseconds
+_SCALE = {"byte": 1.0, "Kbyte": 1e3, "KB": 1e3, "Mbyte": 1e6, "MB": 1e6, "Gbyte": 1e9, "GB": 1e9,
+          "nsecond": 1.0, "ns": 1.0, "usecond": 1e3, "us": 1e3, "msecond": 1e6, "ms": 1e6}
+
+
 def _number(v: str) -> float:
     return float(v.replace(",", ""))
 
@@ -44,19 +49,8 @@ def read_capture(path: str, kernel: str) -> dict:
         if len(r) <= kcol or kernel not in r[kcol]:
             continue
         for m, c in col.items():
-            scale = 1.0
             u = units[c] if c < len(units) else ""
-            if u in ("Kbyte", "KB"):
-                scale = 1e3
-            elif u in ("Mbyte", "MB"):
-                scale = 1e6
-            elif u in ("Gbyte", "GB"):
-                scale = 1e9
-            elif u == "usecond":
-                scale = 1e3
-            elif u == "msecond":
-                scale = 1e6
-            acc[m].append(_number(r[c]) * scale)
+            acc[m].append(_number(r[c]) * _SCALE.get(u, 1.0))
     return {m: sum(v) / len(v) for m, v in acc.items() if v}
 
 
