@@ -23,7 +23,7 @@ namespace {
 constexpr int kChunk = 8;
 
 // ------------------------------------------------------------------ reduce
-// Per-pair FP64 sums of the per-row partials written by k_assoc / k_select / k_rescan.
+// Per-pair FP64 sums of the per-row partials written by k_rowsum.
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(BatchDev B, KParams K) {
   __shared__ double sh[kReduceThreads / 32][10];
   __shared__ bool last;
@@ -332,6 +332,11 @@ static int pick_assoc(AssocFn &a, AssocFn &rs, size_t &smem, int &per_sm) {
       cudaGetLastError();
       return CVO_ERR_CUDA;
     }
+    // the selection keeps kSelBlocksPerSm blocks of static shared memory resident: ask
+    // for the largest shared-memory share of the unified L1 (a hint; failure is harmless)
+    if (cudaFuncSetAttribute(k_select, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+      cudaGetLastError();
     set_mask |= bit;
   }
   static int occ[64] = {0};
@@ -744,7 +749,7 @@ int build_batch(Handle *h, const KParams &K, const std::vector<DevCloud *> &srcs
   const int per_sm = tc.blocks_per_sm > 0 ? std::min(tc.blocks_per_sm, bh->assoc_per_sm) : bh->assoc_per_sm;
   bh->assoc_blocks = std::max(1, std::min(B.total_warps / kCtaWarps, per_sm * (h->num_sms > 0 ? h->num_sms : 152)));
   bh->xform_blocks = (B.total_targets + 255) / 256;
-  bh->sel_blocks = std::max(1, std::min(h->num_sms > 0 ? 4 * h->num_sms : 608, (total_rows + 3) / 4));
+  bh->sel_blocks = std::max(1, std::min(kSelBlocksPerSm * (h->num_sms > 0 ? h->num_sms : 152), (total_rows + 3) / 4));
   return 0;
 }
 
@@ -1131,11 +1136,94 @@ int run_inner_product_batch(Handle *h, DevCloud *src, DevCloud *tgt, const std::
   return 0;
 }
 
+AssocGraph::~AssocGraph() {
+  if (exec) cudaGraphExecDestroy(exec);
+  cudaFreeHost(pin_in);
+  cudaFreeHost(pin_out);
+  cudaFreeHost(pin_err);
+}
+
+namespace {
+
+// Uploads bh's pair records, runs the association and reads the records and the error
+// word back, through g's graph (captured anew when the launch parameters changed).
+int replay_association(Handle *h, BatchHost *bh, const KParams &K, AssocGraph *g) {
+  const int np = bh->B.npairs;
+  if (g->pin_pairs < np) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+    cudaFreeHost(g->pin_in);
+    cudaFreeHost(g->pin_out);
+    cudaFreeHost(g->pin_err);
+    g->pin_in = g->pin_out = nullptr;
+    g->pin_err = nullptr;
+    g->pin_pairs = 0;
+    if (cudaMallocHost((void **)&g->pin_in, sizeof(PairDev) * np) != cudaSuccess ||
+        cudaMallocHost((void **)&g->pin_out, sizeof(PairDev) * np) != cudaSuccess ||
+        cudaMallocHost((void **)&g->pin_err, sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return CVO_ERR_OUT_OF_MEMORY;
+    }
+    g->pin_pairs = np;
+  }
+  std::vector<unsigned char> key;
+  auto add = [&](const void *p, size_t n) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    key.insert(key.end(), c, c + n);
+  };
+  add(&bh->B, sizeof(bh->B));
+  add(&K, sizeof(K));
+  add(&bh->assoc, sizeof(bh->assoc));
+  add(&bh->rescan, sizeof(bh->rescan));
+  add(&bh->assoc_smem, sizeof(bh->assoc_smem));
+  add(&bh->assoc_blocks, sizeof(bh->assoc_blocks));
+  add(&bh->xform_blocks, sizeof(bh->xform_blocks));
+  add(&bh->sel_blocks, sizeof(bh->sel_blocks));
+  add(&g->pin_in, sizeof(g->pin_in));
+  add(&h->stream, sizeof(h->stream));
+  if (!g->exec || g->key != key) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+    const long long before = h->launches;
+    CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = cudaMemcpyAsync(bh->B.pairs, g->pin_in, sizeof(PairDev) * np, cudaMemcpyHostToDevice, h->stream);
+    launch_association(h, bh, K);
+    cudaError_t e2 = cudaMemcpyAsync(g->pin_out, bh->B.pairs, sizeof(PairDev) * np, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e3 = cudaMemcpyAsync(g->pin_err, bh->B.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e4 = cudaStreamEndCapture(h->stream, &graph);
+    g->launches = h->launches - before;
+    h->launches = before;
+    cudaError_t e5 = cudaSuccess;
+    if (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess)
+      e5 = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaError_t e : {e1, e2, e3, e4, e5})
+      if (e != cudaSuccess) {
+        g->exec = nullptr;
+        return set_cuda_error(h, e, "association graph capture");
+      }
+    g->key = key;
+    g->captures++;
+  } else {
+    g->replays++;
+  }
+  memcpy(g->pin_in, bh->pairs.data(), sizeof(PairDev) * np);
+  CVO_CUDA_TRY(h, cudaGraphLaunch(g->exec, h->stream));
+  h->launches += g->launches;
+  CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (*g->pin_err) return *g->pin_err;
+  memcpy(bh->pairs.data(), g->pin_out, sizeof(PairDev) * np);
+  return 0;
+}
+
+}  // namespace
+
 int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
                           const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
                           const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out,
-                          const KParams *kparams) {
+                          const KParams *kparams, AssocGraph *graph) {
   NvtxRange nvtx_range("association_edges");
   const int ne = (int)srcs.size();
   out->assign(ne, EdgeAssoc());
@@ -1166,10 +1254,15 @@ int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const 
       if (P.level_r[i] >= rw) { P.level = i; break; }
     P.level_used = P.level;
   }
-  CVO_CUDA_TRY(h, cudaMemcpyAsync(bh.B.pairs, bh.pairs.data(), sizeof(PairDev) * ne, cudaMemcpyHostToDevice, h->stream));
-  launch_association(h, &bh, K);
-  if ((rc = check_err(h, &bh))) return rc;
-  if ((rc = read_pairs(h, &bh))) return rc;
+  if (graph && !h->prof.on) {
+    if ((rc = replay_association(h, &bh, K, graph))) return rc;
+  } else {
+    CVO_CUDA_TRY(h, cudaMemcpyAsync(bh.B.pairs, bh.pairs.data(), sizeof(PairDev) * ne, cudaMemcpyHostToDevice,
+                                    h->stream));
+    launch_association(h, &bh, K);
+    if ((rc = check_err(h, &bh))) return rc;
+    if ((rc = read_pairs(h, &bh))) return rc;
+  }
   for (int e = 0; e < ne; e++) {
     const PairDev &P = bh.pairs[e];
     EdgeAssoc &A = (*out)[e];

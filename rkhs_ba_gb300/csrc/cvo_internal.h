@@ -280,11 +280,30 @@ struct EdgeAssoc {
   long long nnz;
   int max_row;
 };
+// Replayable launch sequence of an edge-association batch: the upload of the pair
+// records, the association kernels, and the read-back of the records and of the error
+// word, captured once as a CUDA graph and relaunched while the batch's launch
+// parameters are byte-identical.  The pair records travel through pinned staging
+// buffers, whose addresses the graph's copy nodes hold.  One object serves the
+// successive batches of one caller (the outer iterations of a window solve).
+struct AssocGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned char> key;
+  long long launches = 0;       // kernel launches of one replay
+  PairDev *pin_in = nullptr, *pin_out = nullptr;
+  int *pin_err = nullptr;
+  int pin_pairs = 0;
+  int captures = 0, replays = 0;
+  AssocGraph() = default;
+  AssocGraph(const AssocGraph &) = delete;
+  AssocGraph &operator=(const AssocGraph &) = delete;
+  ~AssocGraph();
+};
 int run_association_edges(Handle *h, const std::vector<DevCloud *> &srcs, const std::vector<DevCloud *> &tgts,
                           const std::vector<const float4 *> &src_world, const std::vector<float> &src_world_norm,
                           const std::vector<float> &tgt_pose, const std::vector<float> &ells,
                           const std::vector<int> &caps, int capmax, std::vector<EdgeAssoc> *out,
-                          const KParams *kparams = nullptr);
+                          const KParams *kparams = nullptr, AssocGraph *graph = nullptr);
 
 // Non-isotropic association (cvo_aniso.cu): CSR of the kernel matrix with a 3x3
 // geometric kernel (column-major), first `cap` pairs per row in index order.

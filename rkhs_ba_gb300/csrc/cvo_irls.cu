@@ -231,6 +231,12 @@ bool chol_solve(int n, std::vector<double> &A, std::vector<double> &b) {
   return true;
 }
 
+// Normal equations of the window's residuals at given poses.  One evaluation is the
+// upload of the poses, the accumulation over every kernel-matrix entry of every edge, the
+// per-edge sums and their read-back; it runs as a CUDA graph (one per kind: with or
+// without H and g) that is captured once and replayed by every evaluation of the LM
+// solves until the edges' layout changes.  The poses and sums travel through pinned
+// buffers, whose addresses the graph's copy nodes hold.
 struct Normal {
   Handle *h;
   int nf;
@@ -239,8 +245,64 @@ struct Normal {
   double *poses_d = nullptr;
   double *partial_d = nullptr;
   double *out_d = nullptr;
+  double *poses_pin = nullptr;    // 12 nf
+  double *out_pin = nullptr;      // kNormTerms per edge
+  int out_pin_edges = 0;
   int total_blocks = 0;
-  std::vector<double> out_h;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  std::vector<unsigned char> key[2];
+
+  Normal() = default;
+  Normal(const Normal &) = delete;
+  Normal &operator=(const Normal &) = delete;
+  ~Normal() {
+    for (auto &e : exec)
+      if (e) cudaGraphExecDestroy(e);
+    cudaFree(partial_d);
+    cudaFree(out_d);
+    cudaFree(edges_d);
+    cudaFree(poses_d);
+    cudaFreeHost(poses_pin);
+    cudaFreeHost(out_pin);
+  }
+
+  int record(bool want) {
+    const int ne = (int)edges.size();
+    const int w = want ? 1 : 0;
+    std::vector<unsigned char> k;
+    auto add = [&](const void *p, size_t n) {
+      const unsigned char *c = static_cast<const unsigned char *>(p);
+      k.insert(k.end(), c, c + n);
+    };
+    const void *ptrs[6] = {edges_d, poses_d, partial_d, out_d, poses_pin, out_pin};
+    add(ptrs, sizeof(ptrs));
+    add(&ne, sizeof(ne));
+    add(&total_blocks, sizeof(total_blocks));
+    add(&nf, sizeof(nf));
+    add(&h->stream, sizeof(h->stream));
+    if (exec[w] && key[w] == k) return 0;
+    if (exec[w]) cudaGraphExecDestroy(exec[w]);
+    exec[w] = nullptr;
+    CVO_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = cudaMemcpyAsync(poses_d, poses_pin, sizeof(double) * 12 * nf, cudaMemcpyHostToDevice, h->stream);
+    if (want) k_irls_accum<true><<<total_blocks, kIrlsThreads, 0, h->stream>>>(edges_d, ne, poses_d, partial_d);
+    else k_irls_accum<false><<<total_blocks, kIrlsThreads, 0, h->stream>>>(edges_d, ne, poses_d, partial_d);
+    k_irls_sum<<<ne, 128, 0, h->stream>>>(edges_d, ne, total_blocks, want ? kNormTerms : 1, partial_d, out_d);
+    cudaError_t e2 = cudaMemcpyAsync(out_pin, out_d, sizeof(double) * ne * kNormTerms, cudaMemcpyDeviceToHost,
+                                     h->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
+    cudaError_t e4 = cudaSuccess;
+    if (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) e4 = cudaGraphInstantiate(&exec[w], g, 0);
+    if (g) cudaGraphDestroy(g);
+    for (cudaError_t e : {e1, e2, e3, e4})
+      if (e != cudaSuccess) {
+        exec[w] = nullptr;
+        return set_cuda_error(h, e, "normal-equation graph capture");
+      }
+    key[w] = k;
+    return 0;
+  }
 
   // cost (and, if want, H and g over all 6 nf parameters) at `poses`
   int eval(const double *poses, bool want, std::vector<double> *H, std::vector<double> *g, double *cost) {
@@ -251,16 +313,12 @@ struct Normal {
       g->assign((size_t)6 * nf, 0.0);
     }
     if (ne == 0) return 0;
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(poses_d, poses, sizeof(double) * 12 * nf, cudaMemcpyHostToDevice, h->stream));
-    if (want) k_irls_accum<true><<<total_blocks, kIrlsThreads, 0, h->stream>>>(edges_d, ne, poses_d, partial_d);
-    else k_irls_accum<false><<<total_blocks, kIrlsThreads, 0, h->stream>>>(edges_d, ne, poses_d, partial_d);
-    const int nt = want ? kNormTerms : 1;
-    k_irls_sum<<<ne, 128, 0, h->stream>>>(edges_d, ne, total_blocks, nt, partial_d, out_d);
+    if (int rc = record(want)) return rc;
+    memcpy(poses_pin, poses, sizeof(double) * 12 * nf);
+    CVO_CUDA_TRY(h, cudaGraphLaunch(exec[want ? 1 : 0], h->stream));
     h->launches += 2;
-    out_h.resize((size_t)ne * kNormTerms);
-    CVO_CUDA_TRY(h, cudaMemcpyAsync(out_h.data(), out_d, sizeof(double) * ne * kNormTerms, cudaMemcpyDeviceToHost,
-                                    h->stream));
     CVO_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const double *out_h = out_pin;
     const int D = 6 * nf;
     for (int e = 0; e < ne; e++) {
       const double *o = &out_h[(size_t)e * kNormTerms];
@@ -385,6 +443,15 @@ int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, c
   Normal N;
   N.h = h;
   N.nf = nf;
+  if (cudaMallocHost((void **)&N.poses_pin, sizeof(double) * 12 * nf) != cudaSuccess ||
+      cudaMallocHost((void **)&N.out_pin, sizeof(double) * kNormTerms * ne) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return CVO_ERR_OUT_OF_MEMORY;
+  }
+  // the edge association of every outer iteration replays one captured graph while its
+  // launch parameters stay the same
+  AssocGraph ag;
   // per-edge state (BinaryStateGPU members)
   std::vector<double> ell(ne, (double)p.multiframe_ell_init);
   std::vector<int> nn(ne, p.multiframe_num_neighbors), prev_max(ne, 0), iters_per_ell(ne, 0);
@@ -427,7 +494,10 @@ int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, c
       eell[e] = (float)ell[e];
     }
     std::vector<EdgeAssoc> EA;
-    if ((rc = run_association_edges(h, es, et, ew, enorm, epose, eell, nn, init_nn, &EA))) { cleanup(); return rc; }
+    if ((rc = run_association_edges(h, es, et, ew, enorm, epose, eell, nn, init_nn, &EA, nullptr, &ag))) {
+      cleanup();
+      return rc;
+    }
     int counter = 0;
     N.edges.clear();
     int blk = 0;
@@ -454,6 +524,8 @@ int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, c
     N.total_blocks = blk;
     if ((size_t)blk > max_blocks || !N.partial_d) {
       cudaFree(N.partial_d); cudaFree(N.out_d); cudaFree(N.edges_d); cudaFree(N.poses_d);
+      N.partial_d = N.out_d = N.poses_d = nullptr;
+      N.edges_d = nullptr;
       max_blocks = std::max<size_t>(blk, 1) * 2;
       if (cudaMalloc((void **)&N.partial_d, sizeof(double) * kNormTerms * max_blocks) != cudaSuccess ||
           cudaMalloc((void **)&N.out_d, sizeof(double) * kNormTerms * std::max(ne, 1)) != cudaSuccess ||
@@ -488,7 +560,6 @@ int run_align_multi(Handle *h, int nf, DevCloud *const *clouds, double *poses, c
     if (all_min && change < 1e-5) break;
     if (iter >= p.multiframe_max_iters) break;
   }
-  cudaFree(N.partial_d); cudaFree(N.out_d); cudaFree(N.edges_d); cudaFree(N.poses_d);
   cleanup();
   if (iters) *iters = iter;
   auto t1 = std::chrono::steady_clock::now();

@@ -761,36 +761,42 @@ __global__ void __launch_bounds__(256) k_rowsum(BatchDev B, KParams K) {
 
 // One warp per listed row with cap < count <= cap + ov: its ELL slots hold the
 // first cap kept pairs and its spill list (row-major) the rest, in the order they
-// were kept.  A row of up to kSelStage entries is first staged in shared memory
-// (indices and values, 16-byte loads: many loads in flight per lane), so the rest
-// of the selection touches global memory only to write the result.  A radix select
-// over d = j - jmin (jmin, jmax: the row's smallest and largest kept index; 9-bit
-// digits from the highest bit of jmax - jmin, warp-private histograms) finds the
-// cap-th smallest index r.  Offsetting by jmin spreads the indices over the bins, each
-// lane counts its own run of the list (so one instruction's increments come from
-// different grid cells and rarely collide), and a row whose indices span fewer than 512
-// values needs one pass.  The entries with index <= r (exactly cap: indices
-// are distinct) are compacted in list order into the ELL slots.  Longer rows read
-// their entries from global memory on every pass; the compaction is then in place
-// (an entry is read before any write can reach its slot).
+// were kept.  The indices of a row of up to kSelStage entries are first staged in
+// shared memory (16-byte loads: many loads in flight per lane), so the radix passes
+// read no global memory; the values stay in global memory and are read once, by
+// the compaction, for the kept entries only.  A radix select over d = j - jmin
+// (jmin, jmax: the row's smallest and largest kept index; 9-bit digits from the
+// highest bit of jmax - jmin, warp-private histograms) finds the cap-th smallest
+// index r.  Offsetting by jmin spreads the indices over the bins, each lane counts
+// its own run of the list (so one instruction's increments come from different
+// grid cells and rarely collide), and a row whose indices span fewer than 512 values
+// needs one pass.  The entries with index <= r (exactly cap: indices are distinct)
+// are compacted in list order into the ELL slots, in place: an entry is read before
+// any write can reach its slot, and a __syncwarp between a chunk's reads and its
+// writes orders the lanes' accesses.  Longer rows read their indices from global
+// memory on every pass.  Eight blocks of four warps per SM: 6.2 KB of shared memory
+// per warp and at most 64 registers a thread keep 32 warps resident, which hide the
+// latency of the dependent passes of each warp's rows.
 constexpr int kSelBins = 512;
 constexpr int kSelDigit = 9;
+constexpr int kSelBlocksPerSm = 8;
 // bin b lives at b + b / 16: lane l's scan reads its 16 bins at stride 17 words, on
 // distinct banks
 constexpr int kSelHist = kSelBins + kSelBins / 16;
 __device__ __forceinline__ int sel_bin(int b) { return b + (b >> 4); }
-__global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
+__global__ void __launch_bounds__(kSelThreads, kSelBlocksPerSm) k_select(BatchDev B, KParams K) {
   __shared__ int jbuf_all[kSelThreads / 32][kSelStage];
-  __shared__ float vbuf_all[kSelThreads / 32][kSelStage];
   __shared__ int hist_all[kSelThreads / 32][kSelHist];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *jb = jbuf_all[w];
-  float *vb = vbuf_all[w];
   int *hist = hist_all[w];
   const int count = *B.sel_count;
   const int nwarps = gridDim.x * (kSelThreads / 32);
-  for (int e = blockIdx.x * (kSelThreads / 32) + w; e < count; e += nwarps) {
-    const int4 it = B.sel_list[e];
+  const int e0 = blockIdx.x * (kSelThreads / 32) + w;
+  int4 next = e0 < count ? B.sel_list[e0] : make_int4(0, 0, 0, 0);
+  for (int e = e0; e < count; e += nwarps) {
+    const int4 it = next;            // this row's list entry; the next one is loaded meanwhile
+    if (e + nwarps < count) next = B.sel_list[e + nwarps];
     const PairDev *P = &B.pairs[it.x];
     const int s = it.y, cap = P->cap, ov = P->ov;
     const int E = it.z;
@@ -801,44 +807,54 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
     auto gidx = [&](int t) -> int { return t < cap ? Aj[t] : lst[t - cap].x; };
     int jmin = 0x7FFFFFFF, jmax = -1;
     if (staged) {
-      // ELL part: 4 entries per 16-byte load (rows are 16-byte aligned, the pitch covers
-      // the rounded-up chunk); spill part: 2 entries per load (rows start 16-byte aligned)
+      // ELL part: 4 indices per 16-byte load (rows are 16-byte aligned, the pitch covers
+      // the rounded-up chunk); spill part: 2 entries per 16-byte load (rows start 16-byte
+      // aligned).  Each lane issues up to 4 loads before it stores any: the loads go
+      // through generic pointers, which the compiler must not move past a shared-memory
+      // store, so loads and stores interleaved one by one would wait for memory in turn.
       const int nq = (cap + 3) >> 2;
-#pragma unroll 4
-      for (int q = lane; q < nq; q += 32) {
-        const int4 j4 = reinterpret_cast<const int4 *>(Aj)[q];
-        const float4 a4 = reinterpret_cast<const float4 *>(Av)[q];
-        const int jv[4] = {j4.x, j4.y, j4.z, j4.w};
-        const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+      for (int q0 = lane; q0 < nq; q0 += 128) {
+        int4 j4[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-          if (4 * q + i < cap) {
-            jb[4 * q + i] = jv[i];
-            vb[4 * q + i] = av[i];
-            jmin = min(jmin, jv[i]);
-            jmax = max(jmax, jv[i]);
+        for (int u = 0; u < 4; u++)
+          if (q0 + 32 * u < nq) j4[u] = reinterpret_cast<const int4 *>(Aj)[q0 + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int q = q0 + 32 * u;
+          if (q < nq) {
+            const int jv[4] = {j4[u].x, j4[u].y, j4[u].z, j4[u].w};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if (4 * q + i < cap) {
+                jb[4 * q + i] = jv[i];
+                jmin = min(jmin, jv[i]);
+                jmax = max(jmax, jv[i]);
+              }
           }
+        }
       }
       const int ns = E - cap, np = (ns + 1) >> 1;
-#pragma unroll 4
-      for (int q = lane; q < np; q += 32) {
-        int2 e0, e1 = make_int2(0, 0);
-        if (2 * q + 1 < ns) {
-          const int4 v = reinterpret_cast<const int4 *>(lst)[q];
-          e0 = make_int2(v.x, v.y);
-          e1 = make_int2(v.z, v.w);
-        } else {
-          e0 = lst[2 * q];
+      for (int q0 = lane; q0 < np; q0 += 128) {
+        int4 v4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int q = q0 + 32 * u;
+          if (2 * q + 1 < ns) v4[u] = reinterpret_cast<const int4 *>(lst)[q];
+          else if (2 * q < ns) v4[u] = make_int4(lst[2 * q].x, 0, -1, 0);
         }
-        jb[cap + 2 * q] = e0.x;
-        vb[cap + 2 * q] = __int_as_float(e0.y);
-        jmin = min(jmin, e0.x);
-        jmax = max(jmax, e0.x);
-        if (2 * q + 1 < ns) {
-          jb[cap + 2 * q + 1] = e1.x;
-          vb[cap + 2 * q + 1] = __int_as_float(e1.y);
-          jmin = min(jmin, e1.x);
-          jmax = max(jmax, e1.x);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int q = q0 + 32 * u;
+          if (2 * q < ns) {
+            jb[cap + 2 * q] = v4[u].x;
+            jmin = min(jmin, v4[u].x);
+            jmax = max(jmax, v4[u].x);
+            if (2 * q + 1 < ns) {
+              jb[cap + 2 * q + 1] = v4[u].z;
+              jmin = min(jmin, v4[u].z);
+              jmax = max(jmax, v4[u].z);
+            }
+          }
         }
       }
     } else {
@@ -848,33 +864,33 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
         jmax = max(jmax, j);
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      jmin = min(jmin, __shfl_xor_sync(FULLMASK, jmin, o));
-      jmax = max(jmax, __shfl_xor_sync(FULLMASK, jmax, o));
-    }
+    jmin = __reduce_min_sync(FULLMASK, jmin);
+    jmax = __reduce_max_sync(FULLMASK, jmax);
     __syncwarp();
     auto entry = [&](int t) -> int { return staged ? jb[t] : gidx(t); };
     const int span = jmax - jmin;
     const int bits = span > 0 ? 32 - __clz(span) : 1;
+    // lane l counts the contiguous run of entries l * per .. : neighbouring entries of
+    // the list come from one grid cell and share their high index bits, so the 32
+    // increments of one instruction then go to different bins instead of colliding (an
+    // odd run length keeps the 32 lanes' shared-memory reads on distinct banks)
+    const int per = ((E + 31) >> 5) | 1;
+    const int t_lo = lane * per, t_hi = min(t_lo + per, E);
     int prefix = 0, target = cap;
     for (int hs = bits; hs > 0; hs -= kSelDigit) {
       const int sh = max(hs - kSelDigit, 0), wd = hs - sh;
       for (int b = lane; b < kSelHist; b += 32) hist[b] = 0;
       __syncwarp();
-      // lane l counts the contiguous run of entries l * per .. : neighbouring entries of
-      // the list come from one grid cell and share their high index bits, so the 32
-      // increments of one instruction then go to different bins instead of colliding (an
-      // odd run length keeps the 32 lanes' shared-memory reads on distinct banks)
-      const int per = ((E + 31) >> 5) | 1;
-      for (int i = 0; i < per; i++) {
-        const int t = lane * per + i;
-        if (t < E) {
-          const int d = entry(t) - jmin;
-          if ((d >> hs) == (prefix >> hs)) atomicAdd(&hist[sel_bin((d >> sh) & ((1 << wd) - 1))], 1);
-        }
+      const int want = prefix >> hs, mask = (1 << wd) - 1;
+#pragma unroll 4
+      for (int t = t_lo; t < t_hi; t++) {
+        const int d = entry(t) - jmin;
+        if ((d >> hs) == want) atomicAdd(&hist[sel_bin((d >> sh) & mask)], 1);
       }
       __syncwarp();
+      // lane l owns bins 16 l .. 16 l + 15: their total, an exclusive scan over the lanes,
+      // the lane L whose bins reach target, then the bin inside L's 16 (lanes 0..15 read
+      // one bin each and scan them)
       constexpr int kPer = kSelBins / 32;
       int loc = 0;
 #pragma unroll
@@ -887,37 +903,54 @@ __global__ void __launch_bounds__(kSelThreads) k_select(BatchDev B, KParams K) {
       }
       int L = __ffs(__ballot_sync(FULLMASK, incl >= target)) - 1;
       if (L < 0) L = 31;             // unreachable: the counted entries always reach target
-      int run = __shfl_sync(FULLMASK, incl - loc, L);
-      int bin = L * kPer;
-#pragma unroll 1
-      for (int i = 0; i < kPer; i++) {
-        const int hb = hist[sel_bin(L * kPer + i)];
-        if (run + hb >= target) { bin = L * kPer + i; break; }
-        run += hb;
+      const int before = __shfl_sync(FULLMASK, incl - loc, L);
+      const int hb = lane < kPer ? hist[sel_bin(L * kPer + lane)] : 0;
+      int hin = hb;
+#pragma unroll
+      for (int o = 1; o < kPer; o <<= 1) {
+        const int t = __shfl_up_sync(FULLMASK, hin, o);
+        if (lane >= o) hin += t;
       }
-      prefix |= bin << sh;
+      int i_bin = __ffs(__ballot_sync(FULLMASK, lane < kPer && before + hin >= target)) - 1;
+      if (i_bin < 0) i_bin = kPer - 1;  // unreachable, as above
+      const int run = before + __shfl_sync(FULLMASK, hin - hb, i_bin);
+      prefix |= (L * kPer + i_bin) << sh;
       target -= run;
       __syncwarp();
     }
     const int r = jmin + prefix;   // the cap-th smallest kept index
+    // compaction, 128 entries per round: every lane reads its 4 entries (index, and the
+    // value of a kept one: 4 independent loads in flight), a __syncwarp orders these reads
+    // before the round's writes (which go to slots below the round's end), then the 4
+    // chunks are placed in list order
     int base = 0;
-    for (int t0 = 0; t0 < E; t0 += 32) {
-      const int t = t0 + lane;
-      int j = 0;
-      float a = 0.f;
-      bool k = false;
-      if (t < E) {
-        j = entry(t);
-        k = j <= r;
-        if (k) a = staged ? vb[t] : (t < cap ? Av[t] : __int_as_float(lst[t - cap].y));
+    for (int t0 = 0; t0 < E; t0 += 128) {
+      int j[4];
+      float a[4];
+      bool k[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int t = t0 + 32 * u + lane;
+        j[u] = t < E ? entry(t) : 0;
+        k[u] = t < E && j[u] <= r;
+        a[u] = 0.f;
       }
-      const unsigned bal = __ballot_sync(FULLMASK, k);
-      const int c = base + __popc(bal & ((1u << lane) - 1u));
-      if (k && c < cap) {
-        Aj[c] = j;
-        Av[c] = a;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int t = t0 + 32 * u + lane;
+        if (k[u]) a[u] = t < cap ? Av[t] : __int_as_float(lst[t - cap].y);
       }
-      base += __popc(bal);
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const unsigned bal = __ballot_sync(FULLMASK, k[u]);
+        const int c = base + __popc(bal & ((1u << lane) - 1u));
+        if (k[u] && c < cap) {
+          Aj[c] = j[u];
+          Av[c] = a[u];
+        }
+        base += __popc(bal);
+      }
     }
     __syncwarp();
   }

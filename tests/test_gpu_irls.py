@@ -93,6 +93,26 @@ def test_multiframe_device_clouds_and_no_edges(cuda_device):
     assert it_n == 0 and np.array_equal(Pn, P0)
 
 
+def test_multiframe_graph_replay(cuda_device):
+    """Every outer iteration's edge association and every normal-equation evaluation of
+    the LM solves replay captured CUDA graphs.  A second solve on the same handle (fresh
+    graphs per solve, the same launch parameters) returns the same poses bit for bit, and
+    so does a solve with profiling on, whose edge association launches its kernels
+    directly instead of through the graph."""
+    clouds, gt, P0 = _window(seed=3)
+    p = CvoParams(params_path("irls"))
+    p.multiframe_max_iters = 6
+    cvo = CvoGPU(params=p)
+    hold = [1, 0, 0, 0]
+    P1, _, it1 = cvo.align_multi(clouds, P0, hold, EDGES)
+    P2, _, it2 = cvo.align_multi(clouds, P0, hold, EDGES)
+    assert it1 == it2 and np.array_equal(P1, P2)
+    cvo.profile(True)
+    P3, _, it3 = cvo.align_multi(clouds, P0, hold, EDGES)
+    cvo.profile(False)
+    assert it3 == it1 and np.array_equal(P3, P1)
+
+
 def _window_c4(seed=0):
     """The configured window: 8 frames of 20k-60k colour points along a smooth trajectory
     (0.8 m / 2 deg per step), every frame but the first perturbed by 1 deg / 3 cm, all 28
