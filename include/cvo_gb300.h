@@ -38,7 +38,7 @@ enum {
   CVO_ERR_BAD_YAML = -4,
   CVO_ERR_CUDA = -5,
   CVO_ERR_OUT_OF_MEMORY = -6,
-  CVO_ERR_TIMEOUT = -7,        /* reserved: no kernel of this build waits on another thread or copy */
+  CVO_ERR_TIMEOUT = -7,        /* a bounded device wait gave up (the proposal GEMM's MMA completions); the association kernels wait on nothing */
   CVO_ERR_UNSUPPORTED = -8,
   CVO_ERR_IO = -9,
   CVO_ERR_CAPACITY = -10

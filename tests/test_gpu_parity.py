@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
 
-Tolerances (BASELINE the benchmark spec): neighbour sets bit-exact; inner products and
+Tolerances: neighbour sets bit-exact; inner products and
 kernel values within 1e-5 relative (the GPU evaluates kernel values with FP32
 exp and re-evaluates pairs near the threshold in FP64); final poses within
 1e-4 rad / 1e-4 m of the oracle's trajectory.
